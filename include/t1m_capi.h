@@ -1,0 +1,155 @@
+/* t1m_capi.h — C-ABI of libt1m_cuda.so, the GB300 (sm_103a) contraction engine.
+ *
+ * The reference (MatthiasReumann/t1m) is a header-only C++ library with no FFI;
+ * its public boundary is the pair of t1m::contract templates
+ * (include/t1m/t1m.h:560-568 real, :570-577 complex) over the non-owning
+ * t1m::tensor view (include/t1m/t1m.h:31-66).  This header is the plain-C
+ * surface those templates forward to in this project (include/t1m/t1m.h here
+ * is the drop-in C++ API); every entry point below names the reference
+ * interface it replaces.  No torch or CUDA types appear in the signatures:
+ * streams are passed as void* (a cudaStream_t).
+ *
+ * Ownership: the caller owns every tensor.  Data pointers may be device
+ * pointers (used in place) or host pointers (staged host->device and back by
+ * the library, timed separately in the report).
+ * Errors: every function returns a t1m_status (0 = success); the reference
+ * only throws std::bad_alloc (t1m.h:455-458).
+ * Threading: one context per host thread (or per stream); contexts share
+ * nothing but read-only kernels.
+ */
+#ifndef T1M_CAPI_H
+#define T1M_CAPI_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum t1m_status {
+  T1M_OK = 0,
+  T1M_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad dtype/rank/layout       */
+  T1M_ERR_LABELS = 2,           /* label/extent mismatch, repeated label, a
+                                   label in A, B and C (batch mode)          */
+  T1M_ERR_ALLOC = 3,            /* device or host allocation failed (the
+                                   reference's std::bad_alloc, t1m.h:455-458) */
+  T1M_ERR_CUDA = 4,             /* a CUDA runtime call failed                */
+  T1M_ERR_UNSUPPORTED = 5,      /* method not available for this dtype/shape */
+  T1M_ERR_KERNEL_TIMEOUT = 6,   /* a bounded device-side wait ran out        */
+  T1M_ERR_NO_DEVICE = 7         /* no CUDA device / not an sm_103 device     */
+} t1m_status;
+
+/* Element types: the reference's TensorScalar set (t1m.h:15-23). */
+typedef enum t1m_dtype {
+  T1M_FLOAT32 = 0,
+  T1M_FLOAT64 = 1,
+  T1M_COMPLEX64 = 2,  /* std::complex<float>, interleaved re/im  */
+  T1M_COMPLEX128 = 3  /* std::complex<double>, interleaved re/im */
+} t1m_dtype;
+
+/* Memory layouts.  Values 0/1 match the reference's memory_layout enum
+ * (t1m.h:29: row_major = 0, col_major = 1); the reference leaves row_major
+ * strides uninitialised (t1m.h:51-52), here it is implemented.  T1M_STRIDED
+ * takes explicit element strides. */
+typedef enum t1m_layout {
+  T1M_ROW_MAJOR = 0,
+  T1M_COL_MAJOR = 1,
+  T1M_STRIDED = 2
+} t1m_layout;
+
+/* How the contraction is computed on the GPU.  The reference always runs the
+ * BLIS real micro-kernel on 1M-packed panels (t1m.h:508-554, mappings.h:91-99). */
+typedef enum t1m_method {
+  T1M_METHOD_AUTO = 0,       /* pick per dtype and shape                     */
+  T1M_METHOD_PLAIN = 1,      /* SIMT FP32/FP64 FMA (the plain GPU form)      */
+  T1M_METHOD_TC_3XTF32 = 2,  /* complex64: tcgen05 kind::tf32, hi/lo split,
+                                3 products, FP32 accumulation in TMEM         */
+  T1M_METHOD_TC_BF16X3 = 3,  /* complex64: tcgen05 kind::f16 (bf16), 2-way
+                                split, 3 products                             */
+  T1M_METHOD_TC_BF16X6 = 4,  /* complex64: bf16 3-way split, 6 products      */
+  T1M_METHOD_DMMA = 5        /* complex128/float64: FP64 tensor MMA          */
+} t1m_method;
+
+/* A tensor view: the C form of t1m::tensor<T, ndim> (t1m.h:31-66). */
+typedef struct t1m_tensor {
+  int32_t ndim;            /* number of modes (>= 0)                          */
+  int32_t layout;          /* t1m_layout                                      */
+  const int64_t* extents;  /* ndim extents                                    */
+  const int64_t* strides;  /* ndim element strides; read iff T1M_STRIDED      */
+  void* data;              /* host or device pointer                          */
+} t1m_tensor;
+
+/* Filled by t1m_contract when non-null. */
+typedef struct t1m_report {
+  int32_t method;      /* t1m_method that ran                               */
+  int32_t split_k;     /* K partitions (1 = none)                           */
+  int64_t m, n, k;     /* matricised sizes (products of bundle extents)     */
+  double flops;        /* 8*M*N*K complex, 2*M*N*K real                     */
+  double kernel_ms;    /* device time of the compute kernels (CUDA events)  */
+  double h2d_ms;       /* host->device staging time (0 for device operands) */
+  double d2h_ms;       /* device->host staging time                         */
+  int64_t h2d_bytes;
+  int64_t d2h_bytes;
+  int32_t kernels;     /* kernels launched by this call                     */
+  int32_t reserved;
+} t1m_report;
+
+typedef struct t1m_context t1m_context;
+
+/* Flags for t1m_contract. */
+#define T1M_FLAG_ACCUMULATE 1u /* reference semantics: C <- C + alpha*A*B,
+                                  beta ignored (t1m.h:497-502, 543-548)     */
+#define T1M_FLAG_CONJ_A 2u     /* use conj(A) (adjoint contractions)        */
+#define T1M_FLAG_CONJ_B 4u     /* use conj(B)                               */
+#define T1M_FLAG_NO_TIMING 8u  /* skip the CUDA events of the report        */
+
+/* Create a context on `device` (the BLIS context slot of the reference,
+ * `const cntx_t* cntx = bli_gks_query_cntx()`, t1m.h:566/575, becomes this
+ * handle: stream, method and plan cache). */
+int t1m_create(t1m_context** ctx, int device);
+int t1m_destroy(t1m_context* ctx);
+/* Run on a caller-owned cudaStream_t (NULL = the context's own stream). */
+int t1m_set_stream(t1m_context* ctx, void* stream);
+int t1m_set_method(t1m_context* ctx, int method);
+int t1m_synchronize(t1m_context* ctx);
+const char* t1m_status_string(int status);
+const char* t1m_last_error(const t1m_context* ctx);
+/* Library version and the compute capability it was built for (103). */
+int t1m_version(int* major, int* minor, int* sm);
+
+/* Contract A and B into C by label strings (einstein notation).
+ * Replaces t1m::contract (t1m.h:560-577).
+ *
+ * alpha, beta point to one scalar of `dtype` (complex: re, im).  Without
+ * T1M_FLAG_ACCUMULATE: C <- alpha*A*B + beta*C (BLAS semantics; beta == 0
+ * does not read C).  With it: C <- C + alpha*A*B exactly like the reference
+ * (which ignores beta, and uses alpha = 1 for complex types).
+ * Bundles follow the reference (t1m.h:90-136): contracted = labels of A and B,
+ * free labels of A then B must appear in C.  Unlike the reference, empty
+ * bundles (outer products, full contractions to a 0-mode C) are allowed. */
+int t1m_contract(t1m_context* ctx, int dtype, const void* alpha,
+                 const t1m_tensor* a, const char* labels_a, const t1m_tensor* b,
+                 const char* labels_b, const void* beta, const t1m_tensor* c,
+                 const char* labels_c, uint32_t flags, t1m_report* report);
+
+/* Result of label analysis (no GPU needed). */
+typedef struct t1m_plan_info {
+  int64_t m, n, k;           /* products of the free-A, free-B, contracted extents */
+  int32_t modes_m, modes_n, modes_k;
+  int32_t reserved;
+} t1m_plan_info;
+
+/* Validate labels/extents/strides and report the matricised sizes without
+ * touching the GPU.  Replaces the reference's get_index_bundles and
+ * matrix_layout (t1m.h:90-136, 246-268), with the validation the reference
+ * lacks.  On failure a message is written to err (err_len bytes, may be 0). */
+int t1m_analyze(int dtype, const t1m_tensor* a, const char* labels_a,
+                const t1m_tensor* b, const char* labels_b, const t1m_tensor* c,
+                const char* labels_c, t1m_plan_info* info, char* err,
+                int32_t err_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* T1M_CAPI_H */

@@ -1,0 +1,309 @@
+"""t1m_gb300 — Python host API over libt1m_cuda.so (the C-ABI of include/t1m_capi.h).
+
+Mirrors the reference's public interface (include/t1m/t1m.h):
+
+* ``memory_layout`` with ``row_major`` / ``col_major`` (t1m.h:29),
+* ``tensor(dims, data, layout=col_major)`` — a non-owning view (t1m.h:31-66),
+* ``contract(a, "abc", b, "bd", c, "acd")`` for complex tensors and
+  ``contract(alpha, a, la, b, lb, beta, c, lc)`` for real ones (t1m.h:560-577),
+  with the reference's semantics C <- C + alpha*A*B,
+
+plus ``contract_scaled`` (C <- alpha*A*B + beta*C with complex alpha/beta) and
+the adjoint ``contract_vjp``.  Data may be numpy arrays (host memory, staged by
+the library) or torch tensors / raw device pointers (used in place).
+
+The compute always runs in libt1m_cuda.so on the GPU; there is no CPU path.
+If the library is missing this module raises instead of falling back.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+from dataclasses import dataclass
+from pathlib import Path
+from typing import Any, Sequence
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "libt1m_cuda.so"
+
+# t1m_status
+OK = 0
+_STATUS = {1: "invalid argument", 2: "invalid labels or extents", 3: "allocation failed",
+           4: "CUDA error", 5: "unsupported method", 6: "device-side wait timed out",
+           7: "no usable CUDA device"}
+
+# t1m_dtype
+FLOAT32, FLOAT64, COMPLEX64, COMPLEX128 = 0, 1, 2, 3
+_NP_DTYPE = {FLOAT32: np.float32, FLOAT64: np.float64, COMPLEX64: np.complex64,
+             COMPLEX128: np.complex128}
+_DTYPE_OF = {np.dtype(v): k for k, v in _NP_DTYPE.items()}
+
+FLAG_ACCUMULATE = 1
+FLAG_CONJ_A = 2
+FLAG_CONJ_B = 4
+FLAG_NO_TIMING = 8
+
+
+class memory_layout(enum.IntEnum):
+    """Same values as the reference's enum (t1m.h:29)."""
+    row_major = 0
+    col_major = 1
+
+
+row_major = memory_layout.row_major
+col_major = memory_layout.col_major
+STRIDED = 2
+
+
+class method(enum.IntEnum):
+    auto = 0
+    plain = 1
+    tc_3xtf32 = 2
+    tc_bf16x3 = 3
+    tc_bf16x6 = 4
+    dmma = 5
+
+
+class T1MError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"t1m status {status} ({_STATUS.get(status, '?')}): {message}")
+        self.status = status
+
+
+class _Tensor(C.Structure):
+    _fields_ = [("ndim", C.c_int32), ("layout", C.c_int32),
+                ("extents", C.POINTER(C.c_int64)), ("strides", C.POINTER(C.c_int64)),
+                ("data", C.c_void_p)]
+
+
+class Report(C.Structure):
+    _fields_ = [("method", C.c_int32), ("split_k", C.c_int32), ("m", C.c_int64),
+                ("n", C.c_int64), ("k", C.c_int64), ("flops", C.c_double),
+                ("kernel_ms", C.c_double), ("h2d_ms", C.c_double), ("d2h_ms", C.c_double),
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("kernels", C.c_int32),
+                ("reserved", C.c_int32)]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+class PlanInfo(C.Structure):
+    _fields_ = [("m", C.c_int64), ("n", C.c_int64), ("k", C.c_int64), ("modes_m", C.c_int32),
+                ("modes_n", C.c_int32), ("modes_k", C.c_int32), ("reserved", C.c_int32)]
+
+
+_lib_handle: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    """Load libt1m_cuda.so (raises if it was not built)."""
+    global _lib_handle
+    if _lib_handle is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(
+                f"{LIB_PATH} is missing: build it with `python -c \"import __graft_entry__ as g; g.build()\"`"
+                " (t1m_gb300 has no CPU fallback)")
+        h = C.CDLL(str(LIB_PATH))
+        vp, i32, u32 = C.c_void_p, C.c_int, C.c_uint32
+        h.t1m_create.argtypes = [C.POINTER(vp), i32]
+        h.t1m_destroy.argtypes = [vp]
+        h.t1m_set_stream.argtypes = [vp, vp]
+        h.t1m_set_method.argtypes = [vp, i32]
+        h.t1m_synchronize.argtypes = [vp]
+        h.t1m_status_string.restype = C.c_char_p
+        h.t1m_status_string.argtypes = [i32]
+        h.t1m_last_error.restype = C.c_char_p
+        h.t1m_last_error.argtypes = [vp]
+        h.t1m_version.argtypes = [C.POINTER(C.c_int)] * 3
+        tp = C.POINTER(_Tensor)
+        h.t1m_contract.argtypes = [vp, i32, vp, tp, C.c_char_p, tp, C.c_char_p, vp, tp,
+                                   C.c_char_p, u32, C.POINTER(Report)]
+        h.t1m_analyze.argtypes = [i32, tp, C.c_char_p, tp, C.c_char_p, tp, C.c_char_p,
+                                  C.POINTER(PlanInfo), C.c_char_p, C.c_int32]
+        _lib_handle = h
+    return _lib_handle
+
+
+class Context:
+    """The C-ABI context (replaces the reference's BLIS cntx_t* slot)."""
+
+    def __init__(self, device: int = 0, method_: int | str = method.auto):
+        self._h = C.c_void_p()
+        st = lib().t1m_create(C.byref(self._h), int(device))
+        if st != OK:
+            raise T1MError(st, "t1m_create failed")
+        self.set_method(method_)
+
+    def set_method(self, m: int | str) -> None:
+        if isinstance(m, str):
+            m = method[m]
+        self._check(lib().t1m_set_method(self._h, int(m)))
+
+    def set_stream(self, stream: int | None) -> None:
+        self._check(lib().t1m_set_stream(self._h, stream or None))
+
+    def synchronize(self) -> None:
+        self._check(lib().t1m_synchronize(self._h))
+
+    def _check(self, st: int) -> None:
+        if st != OK:
+            raise T1MError(st, (lib().t1m_last_error(self._h) or b"").decode())
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            lib().t1m_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context()
+    return _default_ctx
+
+
+def _data_ptr(data: Any) -> tuple[int, np.dtype]:
+    if isinstance(data, np.ndarray):
+        return data.ctypes.data, data.dtype
+    try:
+        import torch  # plumbing only: device memory
+        if isinstance(data, torch.Tensor):
+            npdt = {torch.float32: np.float32, torch.float64: np.float64,
+                    torch.complex64: np.complex64, torch.complex128: np.complex128}[data.dtype]
+            return data.data_ptr(), np.dtype(npdt)
+    except ImportError:
+        pass
+    raise TypeError(f"unsupported tensor storage {type(data)!r}")
+
+
+@dataclass
+class tensor:
+    """Non-owning tensor view, like the reference's t1m::tensor (t1m.h:31-66).
+
+    ``data`` is a flat buffer (numpy array, torch tensor) holding the elements
+    in ``layout`` order, or any array together with explicit ``strides``
+    (elements)."""
+    dims: Sequence[int]
+    data: Any
+    layout: int = col_major
+    strides: Sequence[int] | None = None
+
+    def rank(self) -> int:
+        return len(self.dims)
+
+    def dtype(self) -> np.dtype:
+        return _data_ptr(self.data)[1]
+
+    def _c(self, keep: list) -> _Tensor:
+        ptr, _ = _data_ptr(self.data)
+        ext = (C.c_int64 * max(1, len(self.dims)))(*[int(d) for d in self.dims])
+        keep.append(ext)
+        t = _Tensor(len(self.dims), int(self.layout), ext, None, ptr)
+        if self.strides is not None:
+            st = (C.c_int64 * max(1, len(self.strides)))(*[int(s) for s in self.strides])
+            keep.append(st)
+            t.layout = STRIDED
+            t.strides = st
+        return t
+
+    @staticmethod
+    def from_array(arr: np.ndarray) -> "tensor":
+        """View a numpy array with its own strides."""
+        item = arr.itemsize
+        return tensor(arr.shape, arr, STRIDED, [s // item for s in arr.strides])
+
+
+def _scalar_bytes(dtype: int, v) -> C.Array:
+    v = complex(v)
+    if dtype == FLOAT32:
+        return (C.c_float * 1)(v.real)
+    if dtype == FLOAT64:
+        return (C.c_double * 1)(v.real)
+    if dtype == COMPLEX64:
+        return (C.c_float * 2)(v.real, v.imag)
+    return (C.c_double * 2)(v.real, v.imag)
+
+
+def contract_raw(alpha, a: tensor, la: str, b: tensor, lb: str, beta, c: tensor, lc: str,
+                 flags: int = 0, ctx: Context | None = None) -> Report:
+    """One call of t1m_contract; returns its report."""
+    ctx = ctx or default_context()
+    dts = {a.dtype(), b.dtype(), c.dtype()}
+    if len(dts) != 1:
+        raise TypeError(f"mixed element types {dts}")
+    dtype = _DTYPE_OF[dts.pop()]
+    keep: list = []
+    ta, tb, tc = a._c(keep), b._c(keep), c._c(keep)
+    al, be = _scalar_bytes(dtype, alpha), _scalar_bytes(dtype, beta)
+    rep = Report()
+    st = lib().t1m_contract(ctx.handle, dtype, C.cast(al, C.c_void_p), C.byref(ta),
+                            la.encode(), C.byref(tb), lb.encode(), C.cast(be, C.c_void_p),
+                            C.byref(tc), lc.encode(), int(flags), C.byref(rep))
+    if st != OK:
+        raise T1MError(st, (lib().t1m_last_error(ctx.handle) or b"").decode())
+    return rep
+
+
+def contract(*args, ctx: Context | None = None):
+    """Reference-compatible contraction (t1m.h:560-577), C <- C + alpha*A*B.
+
+    ``contract(a, la, b, lb, c, lc)`` for complex tensors;
+    ``contract(alpha, a, la, b, lb, beta, c, lc)`` for real tensors (beta is
+    accepted and ignored, as in the reference)."""
+    if len(args) == 6:
+        a, la, b, lb, c, lc = args
+        if a.dtype().kind != "c":
+            raise TypeError("the 6-argument overload is for complex tensors (t1m.h:570-577)")
+        return contract_raw(1.0, a, la, b, lb, 0.0, c, lc, FLAG_ACCUMULATE, ctx)
+    if len(args) == 8:
+        alpha, a, la, b, lb, beta, c, lc = args
+        if a.dtype().kind == "c":
+            raise TypeError("the 8-argument overload is for real tensors (t1m.h:560-568)")
+        return contract_raw(alpha, a, la, b, lb, beta, c, lc, FLAG_ACCUMULATE, ctx)
+    raise TypeError("contract takes 6 (complex) or 8 (real) positional arguments")
+
+
+def contract_scaled(alpha, a: tensor, la: str, b: tensor, lb: str, beta, c: tensor, lc: str,
+                    ctx: Context | None = None, conj_a: bool = False,
+                    conj_b: bool = False) -> Report:
+    """C <- alpha*op(A)*op(B) + beta*C with complex alpha/beta (no reference
+    counterpart; the reference has no complex scalars, t1m.h:570-577)."""
+    flags = (FLAG_CONJ_A if conj_a else 0) | (FLAG_CONJ_B if conj_b else 0)
+    return contract_raw(alpha, a, la, b, lb, beta, c, lc, flags, ctx)
+
+
+def analyze(a: tensor, la: str, b: tensor, lb: str, c: tensor, lc: str) -> dict:
+    """Label analysis only (no GPU): matricised M, N, K or a T1MError."""
+    dts = {a.dtype(), b.dtype(), c.dtype()}
+    dtype = _DTYPE_OF[dts.pop()] if len(dts) == 1 else -1
+    keep: list = []
+    ta, tb, tc = a._c(keep), b._c(keep), c._c(keep)
+    info = PlanInfo()
+    err = C.create_string_buffer(512)
+    st = lib().t1m_analyze(dtype, C.byref(ta), la.encode(), C.byref(tb), lb.encode(),
+                           C.byref(tc), lc.encode(), C.byref(info), err, 512)
+    if st != OK:
+        raise T1MError(st, err.value.decode())
+    return {"m": info.m, "n": info.n, "k": info.k, "modes": (info.modes_m, info.modes_n,
+                                                              info.modes_k)}
+
+
+def version() -> tuple[int, int, int]:
+    ma, mi, sm = C.c_int(), C.c_int(), C.c_int()
+    lib().t1m_version(C.byref(ma), C.byref(mi), C.byref(sm))
+    return ma.value, mi.value, sm.value

@@ -1,0 +1,477 @@
+// C-ABI of libt1m_cuda.so (declared in include/t1m_capi.h).
+//
+// t1m_contract replaces the reference's t1m::contract (include/t1m/t1m.h:
+// 560-577).  Per call it (1) validates and analyses the labels into a plan of
+// scatter vectors (cached per shape on the device), (2) stages host operands
+// to the device when the caller passed host pointers, (3) launches the kernel
+// of the chosen method on the context's stream, and (4) copies C back for
+// host operands.  Nothing runs on the CPU except label analysis and staging:
+// a missing or failed kernel is an error, never a CPU fallback.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <list>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <unordered_map>
+
+#include "internal.h"
+#include "t1m_capi.h"
+
+using namespace t1m::gb300;
+
+namespace t1m {
+namespace gb300 {
+cudaError_t launch_tc(int method, int dtype, const GemmArgs& args,
+                      const HostPlan& plan, cudaStream_t stream, int* kernels,
+                      std::string* err);
+bool tc_supported(int method, int dtype, const HostPlan& plan);
+}  // namespace gb300
+}  // namespace t1m
+
+struct t1m_context {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  int method = T1M_METHOD_AUTO;
+  std::string last_error;
+  cudaEvent_t ev[6] = {};
+  // Plan cache: key -> (host plan, device scatter vectors), LRU bounded.
+  struct Entry {
+    std::string key;
+    HostPlan host;
+    DevicePlan dev;
+  };
+  std::list<Entry> plans;
+  std::unordered_map<std::string, std::list<Entry>::iterator> index;
+  // Staging buffers for host operands (grow only).
+  void* stage[3] = {nullptr, nullptr, nullptr};
+  size_t stage_bytes[3] = {0, 0, 0};
+};
+
+namespace {
+
+constexpr size_t kMaxPlans = 64;
+
+size_t elem_size(int dtype) {
+  switch (dtype) {
+    case T1M_FLOAT32: return 4;
+    case T1M_FLOAT64: return 8;
+    case T1M_COMPLEX64: return 8;
+    case T1M_COMPLEX128: return 16;
+  }
+  return 0;
+}
+
+int fail(t1m_context* ctx, int status, const std::string& msg) {
+  if (ctx) ctx->last_error = msg;
+  return status;
+}
+
+int cuda_fail(t1m_context* ctx, cudaError_t e, const char* what) {
+  return fail(ctx, T1M_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool resolve_strides(const t1m_tensor* t, int64_t* out) {
+  const int n = t->ndim;
+  if (t->layout == T1M_STRIDED) {
+    if (n > 0 && !t->strides) return false;
+    for (int i = 0; i < n; ++i) out[i] = t->strides[i];
+    return true;
+  }
+  int64_t acc = 1;
+  if (t->layout == T1M_COL_MAJOR) {
+    for (int i = 0; i < n; ++i) { out[i] = acc; acc *= t->extents[i]; }
+    return true;
+  }
+  if (t->layout == T1M_ROW_MAJOR) {
+    for (int i = n - 1; i >= 0; --i) { out[i] = acc; acc *= t->extents[i]; }
+    return true;
+  }
+  return false;
+}
+
+std::string plan_key(int dtype, const t1m_tensor* a, const int64_t* sa, const char* la,
+                     const t1m_tensor* b, const int64_t* sb, const char* lb,
+                     const t1m_tensor* c, const int64_t* sc, const char* lc) {
+  std::string k = std::to_string(dtype);
+  auto add = [&](const t1m_tensor* t, const int64_t* s, const char* l) {
+    k += '|';
+    k += l;
+    for (int i = 0; i < t->ndim; ++i) {
+      k += ',' + std::to_string(t->extents[i]) + ':' + std::to_string(s[i]);
+    }
+  };
+  add(a, sa, la);
+  add(b, sb, lb);
+  add(c, sc, lc);
+  return k;
+}
+
+int upload_plan(t1m_context* ctx, const HostPlan& hp, DevicePlan* dp) {
+  const std::vector<int64_t>* vs[6] = {&hp.rsA, &hp.csA, &hp.rsB, &hp.csB, &hp.rsC, &hp.csC};
+  size_t total = 0;
+  for (auto* v : vs) total += (v->size() + 1) * sizeof(int64_t);
+  void* block = nullptr;
+  cudaError_t e = cudaMalloc(&block, total);
+  if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, std::string("plan allocation: ") + cudaGetErrorString(e));
+  std::vector<int64_t> host;
+  host.reserve(total / sizeof(int64_t));
+  const int64_t* ptrs[6];
+  size_t off = 0;
+  for (int i = 0; i < 6; ++i) {
+    ptrs[i] = static_cast<const int64_t*>(block) + off;
+    host.insert(host.end(), vs[i]->begin(), vs[i]->end());
+    host.push_back(0);
+    off += vs[i]->size() + 1;
+  }
+  e = cudaMemcpy(block, host.data(), total, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(block);
+    return cuda_fail(ctx, e, "plan upload");
+  }
+  dp->block = block;
+  dp->bytes = total;
+  dp->rsA = ptrs[0]; dp->csA = ptrs[1]; dp->rsB = ptrs[2];
+  dp->csB = ptrs[3]; dp->rsC = ptrs[4]; dp->csC = ptrs[5];
+  return T1M_OK;
+}
+
+bool is_device_pointer(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return attr.type == cudaMemoryTypeDevice || attr.type == cudaMemoryTypeManaged;
+}
+
+int ensure_stage(t1m_context* ctx, int i, size_t bytes) {
+  if (ctx->stage_bytes[i] >= bytes) return T1M_OK;
+  if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+  ctx->stage[i] = nullptr;
+  ctx->stage_bytes[i] = 0;
+  cudaError_t e = cudaMalloc(&ctx->stage[i], bytes);
+  if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, std::string("staging allocation: ") + cudaGetErrorString(e));
+  ctx->stage_bytes[i] = bytes;
+  return T1M_OK;
+}
+
+int choose_method(const t1m_context* ctx, int dtype, const HostPlan& plan) {
+  int m = ctx->method;
+  if (m != T1M_METHOD_AUTO) return m;
+  if (dtype == T1M_COMPLEX64 && tc_supported(T1M_METHOD_TC_3XTF32, dtype, plan) &&
+      plan.M * plan.N >= 128 * 256 && plan.K >= 64)
+    return T1M_METHOD_TC_3XTF32;
+  return T1M_METHOD_PLAIN;
+}
+
+}  // namespace
+
+extern "C" {
+
+int t1m_version(int* major, int* minor, int* sm) {
+  if (major) *major = 0;
+  if (minor) *minor = 1;
+  if (sm) *sm = 103;
+  return T1M_OK;
+}
+
+const char* t1m_status_string(int status) {
+  switch (status) {
+    case T1M_OK: return "success";
+    case T1M_ERR_INVALID_ARGUMENT: return "invalid argument";
+    case T1M_ERR_LABELS: return "invalid labels or extents";
+    case T1M_ERR_ALLOC: return "allocation failed";
+    case T1M_ERR_CUDA: return "CUDA error";
+    case T1M_ERR_UNSUPPORTED: return "unsupported method for this contraction";
+    case T1M_ERR_KERNEL_TIMEOUT: return "device-side wait timed out";
+    case T1M_ERR_NO_DEVICE: return "no usable CUDA device";
+  }
+  return "unknown status";
+}
+
+const char* t1m_last_error(const t1m_context* ctx) {
+  return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+int t1m_create(t1m_context** out, int device) {
+  if (!out) return T1M_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= device || device < 0) {
+    cudaGetLastError();
+    return T1M_ERR_NO_DEVICE;
+  }
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return T1M_ERR_NO_DEVICE;
+  if (prop.major != 10 || prop.minor != 3) return T1M_ERR_NO_DEVICE;  // sm_103 only
+  auto* ctx = new (std::nothrow) t1m_context();
+  if (!ctx) return T1M_ERR_ALLOC;
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
+  for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  if (e != cudaSuccess) {
+    t1m_destroy(ctx);
+    return T1M_ERR_CUDA;
+  }
+  ctx->stream = ctx->own_stream;
+  *out = ctx;
+  return T1M_OK;
+}
+
+int t1m_destroy(t1m_context* ctx) {
+  if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (auto& e : ctx->plans) cudaFree(e.dev.block);
+  for (int i = 0; i < 3; ++i)
+    if (ctx->stage[i]) cudaFree(ctx->stage[i]);
+  for (int i = 0; i < 6; ++i)
+    if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return T1M_OK;
+}
+
+int t1m_set_stream(t1m_context* ctx, void* stream) {
+  if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
+  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  return T1M_OK;
+}
+
+int t1m_set_method(t1m_context* ctx, int method) {
+  if (!ctx || method < T1M_METHOD_AUTO || method > T1M_METHOD_DMMA)
+    return T1M_ERR_INVALID_ARGUMENT;
+  ctx->method = method;
+  return T1M_OK;
+}
+
+int t1m_synchronize(t1m_context* ctx) {
+  if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  return e == cudaSuccess ? T1M_OK : cuda_fail(ctx, e, "synchronize");
+}
+
+int t1m_analyze(int dtype, const t1m_tensor* a, const char* la, const t1m_tensor* b,
+                const char* lb, const t1m_tensor* c, const char* lc, t1m_plan_info* info,
+                char* err, int32_t err_len) {
+  auto report = [&](int st, const std::string& msg) {
+    if (err && err_len > 0) {
+      std::strncpy(err, msg.c_str(), static_cast<size_t>(err_len) - 1);
+      err[err_len - 1] = 0;
+    }
+    return st;
+  };
+  if (!a || !b || !c || !la || !lb || !lc) return report(T1M_ERR_INVALID_ARGUMENT, "null argument");
+  if (elem_size(dtype) == 0) return report(T1M_ERR_INVALID_ARGUMENT, "unknown dtype");
+  for (const t1m_tensor* t : {a, b, c}) {
+    if (t->ndim < 0 || t->ndim > 64 || (t->ndim > 0 && !t->extents))
+      return report(T1M_ERR_INVALID_ARGUMENT, "bad tensor rank or extents");
+    if (t->layout < T1M_ROW_MAJOR || t->layout > T1M_STRIDED)
+      return report(T1M_ERR_INVALID_ARGUMENT, "bad layout");
+  }
+  int64_t sa[64], sb[64], sc[64];
+  if (!resolve_strides(a, sa) || !resolve_strides(b, sb) || !resolve_strides(c, sc))
+    return report(T1M_ERR_INVALID_ARGUMENT, "strided tensor without strides");
+  HostPlan hp;
+  std::string msg;
+  const int st = build_plan(dtype, a->ndim, a->extents, sa, la, b->ndim, b->extents, sb, lb,
+                            c->ndim, c->extents, sc, lc, &hp, &msg);
+  if (st != T1M_OK) return report(st, msg);
+  if (info) {
+    info->m = hp.M;
+    info->n = hp.N;
+    info->k = hp.K;
+    info->modes_m = static_cast<int32_t>(hp.modes_m.size());
+    info->modes_n = static_cast<int32_t>(hp.modes_n.size());
+    info->modes_k = static_cast<int32_t>(hp.modes_k.size());
+    info->reserved = 0;
+  }
+  return report(T1M_OK, "");
+}
+
+int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tensor* a,
+                 const char* la, const t1m_tensor* b, const char* lb, const void* beta,
+                 const t1m_tensor* c, const char* lc, uint32_t flags, t1m_report* report) {
+  if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
+  if (!a || !b || !c || !la || !lb || !lc || !alpha || !beta)
+    return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "null argument");
+  const size_t es = elem_size(dtype);
+  if (es == 0) return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "unknown dtype");
+  for (const t1m_tensor* t : {a, b, c}) {
+    if (t->ndim < 0 || t->ndim > 64 || (t->ndim > 0 && !t->extents))
+      return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "bad tensor rank or extents");
+    if (t->layout < T1M_ROW_MAJOR || t->layout > T1M_STRIDED)
+      return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "bad layout");
+  }
+  int64_t sa[64], sb[64], sc[64];
+  if (!resolve_strides(a, sa) || !resolve_strides(b, sb) || !resolve_strides(c, sc))
+    return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "strided tensor without strides");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "set device");
+
+  // Plan (cached).
+  const std::string key = plan_key(dtype, a, sa, la, b, sb, lb, c, sc, lc);
+  t1m_context::Entry* entry = nullptr;
+  auto it = ctx->index.find(key);
+  if (it != ctx->index.end()) {
+    ctx->plans.splice(ctx->plans.begin(), ctx->plans, it->second);
+    entry = &*ctx->plans.begin();
+  } else {
+    t1m_context::Entry fresh;
+    fresh.key = key;
+    std::string err;
+    int st = build_plan(dtype, a->ndim, a->extents, sa, la, b->ndim, b->extents, sb, lb,
+                        c->ndim, c->extents, sc, lc, &fresh.host, &err);
+    if (st != T1M_OK) return fail(ctx, st, err);
+    st = upload_plan(ctx, fresh.host, &fresh.dev);
+    if (st != T1M_OK) return st;
+    ctx->plans.push_front(std::move(fresh));
+    ctx->index[key] = ctx->plans.begin();
+    entry = &*ctx->plans.begin();
+    while (ctx->plans.size() > kMaxPlans) {
+      auto& last = ctx->plans.back();
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(last.dev.block);
+      ctx->index.erase(last.key);
+      ctx->plans.pop_back();
+    }
+  }
+  const HostPlan& hp = entry->host;
+  const DevicePlan& dp = entry->dev;
+
+  if (hp.spanC > 0 && !c->data) return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "null C data");
+  if (hp.M > 0 && hp.N > 0 && hp.K > 0 && (!a->data || !b->data))
+    return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "null A or B data");
+
+  const int method = choose_method(ctx, dtype, hp);
+  const bool timing = report && !(flags & T1M_FLAG_NO_TIMING);
+  const bool cplx = dtype == T1M_COMPLEX64 || dtype == T1M_COMPLEX128;
+
+  // Scalars (the reference's complex overload has alpha = 1, t1m.h:576).
+  GemmArgs g{};
+  g.M = hp.M; g.N = hp.N; g.K = hp.K;
+  g.rsA = dp.rsA; g.csA = dp.csA; g.rsB = dp.rsB; g.csB = dp.csB;
+  g.rsC = dp.rsC; g.csC = dp.csC;
+  g.uA_m = hp.uA_m; g.uA_k = hp.uA_k; g.uB_k = hp.uB_k; g.uB_n = hp.uB_n;
+  g.uC_m = hp.uC_m; g.uC_n = hp.uC_n;
+  auto read_scalar = [&](const void* p, double* out) {
+    switch (dtype) {
+      case T1M_FLOAT32: out[0] = *static_cast<const float*>(p); out[1] = 0; break;
+      case T1M_FLOAT64: out[0] = *static_cast<const double*>(p); out[1] = 0; break;
+      case T1M_COMPLEX64: out[0] = static_cast<const float*>(p)[0]; out[1] = static_cast<const float*>(p)[1]; break;
+      case T1M_COMPLEX128: out[0] = static_cast<const double*>(p)[0]; out[1] = static_cast<const double*>(p)[1]; break;
+    }
+  };
+  read_scalar(alpha, g.alpha);
+  read_scalar(beta, g.beta);
+  g.flags = 0;
+  if (flags & T1M_FLAG_ACCUMULATE) g.flags |= kFlagAccumulate;
+  if ((flags & T1M_FLAG_CONJ_A) && cplx) g.flags |= kFlagConjA;
+  if ((flags & T1M_FLAG_CONJ_B) && cplx) g.flags |= kFlagConjB;
+  if (!(flags & T1M_FLAG_ACCUMULATE) && g.beta[0] == 0.0 && g.beta[1] == 0.0)
+    g.flags |= kFlagBetaZero;
+
+  // Host operands are staged.
+  const bool devA = is_device_pointer(a->data), devB = is_device_pointer(b->data),
+             devC = is_device_pointer(c->data);
+  const size_t bytesA = static_cast<size_t>(hp.spanA) * es;
+  const size_t bytesB = static_cast<size_t>(hp.spanB) * es;
+  const size_t bytesC = static_cast<size_t>(hp.spanC) * es;
+  const bool readC = (g.flags & kFlagAccumulate) || !(g.flags & kFlagBetaZero) || hp.K == 0;
+  int64_t h2d = 0, d2h = 0;
+  cudaStream_t s = ctx->stream;
+  if (timing) cudaEventRecord(ctx->ev[0], s);
+  g.A = a->data;
+  g.B = b->data;
+  g.C = c->data;
+  if (!devA && bytesA) {
+    if (int st = ensure_stage(ctx, 0, bytesA)) return st;
+    if ((e = cudaMemcpyAsync(ctx->stage[0], a->data, bytesA, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return cuda_fail(ctx, e, "copy A to device");
+    g.A = ctx->stage[0];
+    h2d += bytesA;
+  }
+  if (!devB && bytesB) {
+    if (int st = ensure_stage(ctx, 1, bytesB)) return st;
+    if ((e = cudaMemcpyAsync(ctx->stage[1], b->data, bytesB, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+      return cuda_fail(ctx, e, "copy B to device");
+    g.B = ctx->stage[1];
+    h2d += bytesB;
+  }
+  if (!devC && bytesC) {
+    if (int st = ensure_stage(ctx, 2, bytesC)) return st;
+    if (readC || hp.spanC != hp.M * hp.N) {
+      // C's gaps (strided C) must survive the copy back, so it is read too.
+      if ((e = cudaMemcpyAsync(ctx->stage[2], c->data, bytesC, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return cuda_fail(ctx, e, "copy C to device");
+      h2d += bytesC;
+    }
+    g.C = ctx->stage[2];
+  }
+  if (timing) cudaEventRecord(ctx->ev[1], s);
+
+  int kernels = 0;
+  int used_method = method;
+  if (hp.M > 0 && hp.N > 0) {
+    if (hp.K == 0) {
+      // C <- beta*C (or unchanged): nothing to multiply; handled by the plain
+      // kernel with an empty K loop.
+      e = launch_simt(dtype, g, s, &kernels);
+      used_method = T1M_METHOD_PLAIN;
+    } else if (method == T1M_METHOD_PLAIN) {
+      e = launch_simt(dtype, g, s, &kernels);
+    } else {
+      std::string err;
+      if (!tc_supported(method, dtype, hp))
+        return fail(ctx, T1M_ERR_UNSUPPORTED,
+                    std::string("method ") + std::to_string(method) +
+                        " is not available for this dtype/contraction");
+      e = launch_tc(method, dtype, g, hp, s, &kernels, &err);
+      if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
+  }
+  if (timing) cudaEventRecord(ctx->ev[2], s);
+  if (!devC && bytesC) {
+    if ((e = cudaMemcpyAsync(c->data, ctx->stage[2], bytesC, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      return cuda_fail(ctx, e, "copy C to host");
+    d2h += bytesC;
+  }
+  if (timing) cudaEventRecord(ctx->ev[3], s);
+  const bool host_result = (!devC && bytesC);
+  if (host_result || timing) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "contraction");
+  }
+  if (report) {
+    std::memset(report, 0, sizeof(*report));
+    report->method = used_method;
+    report->split_k = 1;
+    report->m = hp.M;
+    report->n = hp.N;
+    report->k = hp.K;
+    report->flops = (cplx ? 8.0 : 2.0) * double(hp.M) * double(hp.N) * double(hp.K);
+    report->h2d_bytes = h2d;
+    report->d2h_bytes = d2h;
+    report->kernels = kernels;
+    if (timing) {
+      float t01 = 0, t12 = 0, t23 = 0;
+      cudaEventElapsedTime(&t01, ctx->ev[0], ctx->ev[1]);
+      cudaEventElapsedTime(&t12, ctx->ev[1], ctx->ev[2]);
+      cudaEventElapsedTime(&t23, ctx->ev[2], ctx->ev[3]);
+      report->h2d_ms = t01;
+      report->kernel_ms = t12;
+      report->d2h_ms = t23;
+    }
+  }
+  return T1M_OK;
+}
+
+}  // extern "C"

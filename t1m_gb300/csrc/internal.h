@@ -1,0 +1,80 @@
+// Internal declarations shared by the host plan builder, the C-ABI and the
+// kernels of libt1m_cuda.so.  Nothing here is part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace t1m {
+namespace gb300 {
+
+// One mode of a bundle as seen by the two tensors that share it.
+//   M bundle: s0 = stride in A, s1 = stride in C
+//   N bundle: s0 = stride in B, s1 = stride in C
+//   K bundle: s0 = stride in A, s1 = stride in B
+struct Mode {
+  int64_t extent;
+  int64_t s0;
+  int64_t s1;
+  char label;
+};
+
+// Host-side description of one contraction after label analysis.
+// Element (m, n) of the matricised problem lives at
+//   A: rsA[m] + csA[k]   B: rsB[k] + csB[n]   C: rsC[m] + csC[n]
+// (the reference's rscat/cscat vectors, t1m.h:141-174, in element units).
+struct HostPlan {
+  int dtype = 0;
+  int64_t M = 0, N = 0, K = 0;
+  std::vector<Mode> modes_m, modes_n, modes_k;
+  std::vector<int64_t> rsA, csA, rsB, csB, rsC, csC;
+  // Uniform stride of each scatter vector, or -1 when it is not an arithmetic
+  // progression (the block-scatter "constant stride" of t1m.h:179-205 taken
+  // over the whole vector).
+  int64_t uA_m = -1, uA_k = -1, uB_k = -1, uB_n = -1, uC_m = -1, uC_n = -1;
+  // Number of elements each tensor spans in memory (1 + sum (e-1)*s).
+  int64_t spanA = 0, spanB = 0, spanC = 0;
+};
+
+// Validate labels/extents/strides and build the plan.  Returns a t1m_status
+// and fills *err with a message on failure.
+int build_plan(int dtype, int na, const int64_t* ea, const int64_t* sa,
+               const char* la, int nb, const int64_t* eb, const int64_t* sb,
+               const char* lb, int nc, const int64_t* ec, const int64_t* sc,
+               const char* lc, HostPlan* plan, std::string* err);
+
+// Device-resident copy of a plan's scatter vectors (one allocation).
+struct DevicePlan {
+  void* block = nullptr;
+  size_t bytes = 0;
+  const int64_t *rsA = nullptr, *csA = nullptr, *rsB = nullptr, *csB = nullptr,
+                *rsC = nullptr, *csC = nullptr;
+};
+
+// Kernel arguments of one contraction launch (plain or tensor-core).
+struct GemmArgs {
+  const void* A;
+  const void* B;
+  void* C;
+  int64_t M, N, K;
+  const int64_t *rsA, *csA, *rsB, *csB, *rsC, *csC;
+  int64_t uA_m, uA_k, uB_k, uB_n, uC_m, uC_n;
+  double alpha[2];
+  double beta[2];
+  uint32_t flags;  // kFlag* below
+};
+
+constexpr uint32_t kFlagAccumulate = 1u;  // C += alpha*AB (beta ignored)
+constexpr uint32_t kFlagConjA = 2u;
+constexpr uint32_t kFlagConjB = 4u;
+constexpr uint32_t kFlagBetaZero = 16u;  // BLAS semantics with beta == 0
+
+// Launchers (simt.cu).  Return cudaError_t of the launch.
+cudaError_t launch_simt(int dtype, const GemmArgs& args, cudaStream_t stream,
+                        int* kernels);
+
+}  // namespace gb300
+}  // namespace t1m

@@ -1,0 +1,270 @@
+// Plain GPU form: SIMT FP32 / FP64 block-scatter contraction kernels.
+//
+// This replaces the reference's BLIS five-loop GEMM (include/t1m/t1m.h:432-557)
+// for the plain method.  One CTA computes a BM x BN tile of the matricised C;
+// A and B tiles are gathered straight from the tensors through the scatter
+// vectors (no packed copy in HBM), staged in shared memory, and multiplied with
+// FMA.  For complex types each complex multiply-add is the 1M real product
+// pair (re*re - im*im, re*im + im*re, t1m.h:309-337) done in registers.
+// The epilogue scatter-writes C with alpha/beta (reference semantics
+// C += alpha*A*B under kFlagAccumulate, t1m.h:406-430).
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "internal.h"
+
+namespace t1m {
+namespace gb300 {
+namespace {
+
+template <class T> struct Scalar;
+template <> struct Scalar<float> {
+  using real = float;
+  static constexpr bool cplx = false;
+};
+template <> struct Scalar<double> {
+  using real = double;
+  static constexpr bool cplx = false;
+};
+template <> struct Scalar<float2> {
+  using real = float;
+  static constexpr bool cplx = true;
+};
+template <> struct Scalar<double2> {
+  using real = double;
+  static constexpr bool cplx = true;
+};
+
+template <class T> __device__ __forceinline__ T zero();
+template <> __device__ __forceinline__ float zero<float>() { return 0.f; }
+template <> __device__ __forceinline__ double zero<double>() { return 0.0; }
+template <> __device__ __forceinline__ float2 zero<float2>() { return make_float2(0.f, 0.f); }
+template <> __device__ __forceinline__ double2 zero<double2>() { return make_double2(0.0, 0.0); }
+
+__device__ __forceinline__ float conj_if(float v, bool) { return v; }
+__device__ __forceinline__ double conj_if(double v, bool) { return v; }
+__device__ __forceinline__ float2 conj_if(float2 v, bool c) { if (c) v.y = -v.y; return v; }
+__device__ __forceinline__ double2 conj_if(double2 v, bool c) { if (c) v.y = -v.y; return v; }
+
+// acc += a * b
+__device__ __forceinline__ void mac(float& acc, float a, float b) { acc = fmaf(a, b, acc); }
+__device__ __forceinline__ void mac(double& acc, double a, double b) { acc = fma(a, b, acc); }
+__device__ __forceinline__ void mac(float2& acc, float2 a, float2 b) {
+  acc.x = fmaf(a.x, b.x, acc.x);
+  acc.x = fmaf(-a.y, b.y, acc.x);
+  acc.y = fmaf(a.y, b.x, acc.y);
+  acc.y = fmaf(a.x, b.y, acc.y);
+}
+__device__ __forceinline__ void mac(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.y, b.x, acc.y);
+  acc.y = fma(a.x, b.y, acc.y);
+}
+
+template <class T> __device__ __forceinline__ T scal(const double* s);
+template <> __device__ __forceinline__ float scal<float>(const double* s) { return (float)s[0]; }
+template <> __device__ __forceinline__ double scal<double>(const double* s) { return s[0]; }
+template <> __device__ __forceinline__ float2 scal<float2>(const double* s) { return make_float2((float)s[0], (float)s[1]); }
+template <> __device__ __forceinline__ double2 scal<double2>(const double* s) { return make_double2(s[0], s[1]); }
+
+__device__ __forceinline__ float mul(float a, float b) { return a * b; }
+__device__ __forceinline__ double mul(double a, double b) { return a * b; }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double2 mul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float add(float a, float b) { return a + b; }
+__device__ __forceinline__ double add(double a, double b) { return a + b; }
+__device__ __forceinline__ float2 add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 add(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+
+__device__ __forceinline__ int64_t offs(const int64_t* v, int64_t u, int64_t i) {
+  return u >= 0 ? i * u : __ldg(v + i);
+}
+
+constexpr int kThreads = 256;
+
+// 16 x 16 threads; thread (tx, ty) owns rows ty*TM .. ty*TM+TM-1 of the tile
+// and columns tx + 16*j (j < TN), so shared-memory reads of B are
+// consecutive across a half-warp and reads of A are broadcasts.
+template <class T, int TM, int TN, int BK>
+__global__ void __launch_bounds__(kThreads)
+simt_contract(const GemmArgs args) {
+  constexpr int BM = 16 * TM;
+  constexpr int BN = 16 * TN;
+  constexpr int A_PER = BM * BK / kThreads;
+  constexpr int B_PER = BN * BK / kThreads;
+  static_assert(A_PER * kThreads == BM * BK, "A tile not divisible");
+  static_assert(B_PER * kThreads == BN * BK, "B tile not divisible");
+
+  __shared__ T As[2][BK][BM];
+  __shared__ T Bs[2][BK][BN];
+  __shared__ int64_t rowA[BM];
+  __shared__ int64_t colB[BN];
+
+  const T* __restrict__ A = static_cast<const T*>(args.A);
+  const T* __restrict__ B = static_cast<const T*>(args.B);
+  T* __restrict__ C = static_cast<T*>(args.C);
+  const int64_t M = args.M, N = args.N, K = args.K;
+  const bool conjA = args.flags & kFlagConjA;
+  const bool conjB = args.flags & kFlagConjB;
+
+  // Tile order: groups of 8 M-tiles sweep N so neighbouring CTAs share B.
+  const int64_t tiles_m = (M + BM - 1) / BM;
+  const int64_t tiles_n = (N + BN - 1) / BN;
+  const int64_t t = blockIdx.x;
+  constexpr int64_t G = 8;
+  const int64_t group = t / (G * tiles_n);
+  const int64_t first_m = group * G;
+  const int64_t gsize = min(G, tiles_m - first_m);
+  const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
+  const int64_t tn = (t % (G * tiles_n)) / gsize;
+  const int64_t m0 = tm * BM, n0 = tn * BN;
+
+  const int tid = threadIdx.x;
+  const int tx = tid % 16, ty = tid / 16;
+
+  for (int i = tid; i < BM; i += kThreads)
+    rowA[i] = (m0 + i < M) ? offs(args.rsA, args.uA_m, m0 + i) : 0;
+  for (int i = tid; i < BN; i += kThreads)
+    colB[i] = (n0 + i < N) ? offs(args.csB, args.uB_n, n0 + i) : 0;
+  __syncthreads();
+
+  // Thread -> element maps of the tile loads: the unit-stride direction of
+  // each operand is the fast thread direction (coalesced gathers).
+  const bool a_kfast = (args.uA_k == 1);
+  const bool b_kfast = (args.uB_k == 1) || (args.uB_n != 1);
+
+  T ra[A_PER], rb[B_PER];
+  auto load_tiles = [&](int64_t k0) {
+#pragma unroll
+    for (int p = 0; p < A_PER; ++p) {
+      const int idx = tid + p * kThreads;
+      const int m = a_kfast ? idx / BK : idx % BM;
+      const int k = a_kfast ? idx % BK : idx / BM;
+      T v = zero<T>();
+      if (m0 + m < M && k0 + k < K)
+        v = conj_if(A[rowA[m] + offs(args.csA, args.uA_k, k0 + k)], conjA);
+      ra[p] = v;
+    }
+#pragma unroll
+    for (int p = 0; p < B_PER; ++p) {
+      const int idx = tid + p * kThreads;
+      const int n = b_kfast ? idx / BK : idx % BN;
+      const int k = b_kfast ? idx % BK : idx / BN;
+      T v = zero<T>();
+      if (n0 + n < N && k0 + k < K)
+        v = conj_if(B[offs(args.rsB, args.uB_k, k0 + k) + colB[n]], conjB);
+      rb[p] = v;
+    }
+  };
+  auto store_tiles = [&](int buf) {
+#pragma unroll
+    for (int p = 0; p < A_PER; ++p) {
+      const int idx = tid + p * kThreads;
+      const int m = a_kfast ? idx / BK : idx % BM;
+      const int k = a_kfast ? idx % BK : idx / BM;
+      As[buf][k][m] = ra[p];
+    }
+#pragma unroll
+    for (int p = 0; p < B_PER; ++p) {
+      const int idx = tid + p * kThreads;
+      const int n = b_kfast ? idx / BK : idx % BN;
+      const int k = b_kfast ? idx % BK : idx / BN;
+      Bs[buf][k][n] = rb[p];
+    }
+  };
+
+  T acc[TM][TN];
+#pragma unroll
+  for (int i = 0; i < TM; ++i)
+#pragma unroll
+    for (int j = 0; j < TN; ++j) acc[i][j] = zero<T>();
+
+  const int64_t ksteps = (K + BK - 1) / BK;
+  if (ksteps > 0) {
+    load_tiles(0);
+    store_tiles(0);
+  }
+  __syncthreads();
+  for (int64_t s = 0; s < ksteps; ++s) {
+    const int buf = static_cast<int>(s & 1);
+    if (s + 1 < ksteps) load_tiles((s + 1) * BK);
+#pragma unroll
+    for (int k = 0; k < BK; ++k) {
+      T a[TM], b[TN];
+#pragma unroll
+      for (int i = 0; i < TM; ++i) a[i] = As[buf][k][ty * TM + i];
+#pragma unroll
+      for (int j = 0; j < TN; ++j) b[j] = Bs[buf][k][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < TM; ++i)
+#pragma unroll
+        for (int j = 0; j < TN; ++j) mac(acc[i][j], a[i], b[j]);
+    }
+    if (s + 1 < ksteps) store_tiles(buf ^ 1);
+    __syncthreads();
+  }
+
+  // Epilogue: scatter-write C with alpha/beta.
+  const T alpha = scal<T>(args.alpha);
+  const T beta = scal<T>(args.beta);
+  const bool accumulate = args.flags & kFlagAccumulate;
+  const bool beta_zero = args.flags & kFlagBetaZero;
+  int64_t colC[TN];
+#pragma unroll
+  for (int j = 0; j < TN; ++j) {
+    const int64_t n = n0 + tx + 16 * j;
+    colC[j] = n < N ? offs(args.csC, args.uC_n, n) : 0;
+  }
+#pragma unroll
+  for (int i = 0; i < TM; ++i) {
+    const int64_t m = m0 + ty * TM + i;
+    if (m >= M) continue;
+    const int64_t r = offs(args.rsC, args.uC_m, m);
+#pragma unroll
+    for (int j = 0; j < TN; ++j) {
+      const int64_t n = n0 + tx + 16 * j;
+      if (n >= N) continue;
+      T* p = C + r + colC[j];
+      const T ab = mul(alpha, acc[i][j]);
+      if (accumulate)
+        *p = add(*p, ab);
+      else if (beta_zero)
+        *p = ab;
+      else
+        *p = add(ab, mul(beta, *p));
+    }
+  }
+}
+
+template <class T, int TM, int TN, int BK>
+cudaError_t launch(const GemmArgs& args, cudaStream_t stream) {
+  constexpr int BM = 16 * TM, BN = 16 * TN;
+  const int64_t tiles = ((args.M + BM - 1) / BM) * ((args.N + BN - 1) / BN);
+  if (tiles == 0) return cudaSuccess;
+  if (tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  simt_contract<T, TM, TN, BK><<<static_cast<unsigned>(tiles), kThreads, 0, stream>>>(args);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_simt(int dtype, const GemmArgs& args, cudaStream_t stream,
+                        int* kernels) {
+  *kernels = 1;
+  switch (dtype) {
+    case 0: return launch<float, 8, 8, 8>(args, stream);
+    case 1: return launch<double, 8, 4, 8>(args, stream);
+    case 2: return launch<float2, 4, 8, 8>(args, stream);
+    case 3: return launch<double2, 4, 4, 8>(args, stream);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace gb300
+}  // namespace t1m
