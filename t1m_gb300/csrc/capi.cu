@@ -26,8 +26,8 @@ using namespace t1m::gb300;
 namespace t1m {
 namespace gb300 {
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args,
-                      const HostPlan& plan, cudaStream_t stream, int* kernels,
-                      std::string* err);
+                      const HostPlan& plan, cudaStream_t stream, int* err_flag,
+                      int* kernels, std::string* err);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
 }  // namespace gb300
 }  // namespace t1m
@@ -39,6 +39,8 @@ struct t1m_context {
   int method = T1M_METHOD_AUTO;
   std::string last_error;
   cudaEvent_t ev[6] = {};
+  // Device-side error word written by kernels whose bounded waits ran out.
+  int* d_err = nullptr;
   // Plan cache: key -> (host plan, device scatter vectors), LRU bounded.
   struct Entry {
     std::string key;
@@ -161,6 +163,17 @@ int ensure_stage(t1m_context* ctx, int i, size_t bytes) {
   return T1M_OK;
 }
 
+// Read (and clear) the kernels' error word; only called after a stream sync.
+int check_device_error(t1m_context* ctx) {
+  int code = 0;
+  cudaError_t e = cudaMemcpy(&code, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "read kernel status");
+  if (code == 0) return T1M_OK;
+  cudaMemset(ctx->d_err, 0, sizeof(int));
+  return fail(ctx, T1M_ERR_KERNEL_TIMEOUT,
+              "a bounded device-side wait timed out (kernel code " + std::to_string(code) + ")");
+}
+
 int choose_method(const t1m_context* ctx, int dtype, const HostPlan& plan) {
   int m = ctx->method;
   if (m != T1M_METHOD_AUTO) return m;
@@ -216,6 +229,8 @@ int t1m_create(t1m_context** out, int device) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, 64);
+  if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 64);
   if (e != cudaSuccess) {
     t1m_destroy(ctx);
     return T1M_ERR_CUDA;
@@ -234,6 +249,7 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->stage[i]) cudaFree(ctx->stage[i]);
   for (int i = 0; i < 6; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return T1M_OK;
@@ -255,7 +271,8 @@ int t1m_set_method(t1m_context* ctx, int method) {
 int t1m_synchronize(t1m_context* ctx) {
   if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
-  return e == cudaSuccess ? T1M_OK : cuda_fail(ctx, e, "synchronize");
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+  return check_device_error(ctx);
 }
 
 int t1m_analyze(int dtype, const t1m_tensor* a, const char* la, const t1m_tensor* b,
@@ -433,7 +450,7 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
         return fail(ctx, T1M_ERR_UNSUPPORTED,
                     std::string("method ") + std::to_string(method) +
                         " is not available for this dtype/contraction");
-      e = launch_tc(method, dtype, g, hp, s, &kernels, &err);
+      e = launch_tc(method, dtype, g, hp, s, ctx->d_err, &kernels, &err);
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
@@ -449,6 +466,7 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
   if (host_result || timing) {
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "contraction");
+    if (int st = check_device_error(ctx)) return st;
   }
   if (report) {
     std::memset(report, 0, sizeof(*report));
