@@ -159,3 +159,43 @@ __device__ __forceinline__ float tf32_rna(float x) {
 }  // namespace ptx
 }  // namespace gb300
 }  // namespace t1m
+
+namespace t1m {
+namespace gb300 {
+namespace ptx {
+
+// ------------------------------------------------------------------ TMA ---
+// 2-D tiled bulk tensor load into this CTA's shared memory; completion is
+// reported as transaction bytes on `bar`.  The innermost coordinate c0 times
+// the element size must be a multiple of 16 bytes (callers use multiples of
+// 32 floats).
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const void* tmap, int c0, int c1,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(tmap)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_prefetch_desc(const void* tmap) {
+  asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(tmap)) : "memory");
+}
+
+// 8-byte asynchronous copy global -> shared; src_bytes = 0 writes zeros
+// without reading the source.
+__device__ __forceinline__ void cp_async_8(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+
+// Arrive on `bar` once all prior cp.async of this thread have landed (the
+// arrival counts against the barrier's initial count).
+__device__ __forceinline__ void cp_async_arrive_noinc(uint32_t bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+}  // namespace ptx
+}  // namespace gb300
+}  // namespace t1m

@@ -5,32 +5,51 @@
 // its BLIS micro-kernel (bli/mappings.h:91-99).  The reference packs complex A
 // into real 2x2 blocks [re -im; im re] and complex B into re/im row pairs
 // (t1m.h:309-337), then runs a real GEMM of size 2M x N x 2K.  Here the same
-// real GEMM runs on the 5th-generation tensor cores:
+// real GEMM runs on the 5th-generation tensor cores, with no packed copy of
+// any tensor in HBM:
 //
-//  * A (1M-expanded, 2 real rows per complex row): producer warps gather
-//    complex A straight from the tensor through the scatter vectors, build the
-//    rows [re, -im, ...] and [im, re, ...], split each value into TF32 hi and
-//    lo parts (hi = rna(x), lo = rna(x - hi)), and store both into TENSOR
-//    MEMORY with tcgen05.st.  The 4x-expanded operand never exists in shared
-//    or global memory.
-//  * B (K-major, re/im interleaved along K, which is exactly the 1M B panel):
-//    producers gather it, split hi/lo and store it into shared memory in the
-//    128-byte-swizzled K-major layout the MMA descriptors read.
-//  * One thread issues tcgen05.mma kind::tf32 (M = 128 real rows = 64 complex
-//    rows, N = 256 complex columns, K = 8): A_hi*B_hi + A_hi*B_lo + A_lo*B_hi
-//    into one FP32 accumulator in TMEM (256 columns).
-//  * The epilogue reads the accumulator with tcgen05.ld; real rows 2i / 2i+1
-//    are re / im of complex row i (t1m.h:425-426), paired across neighbouring
-//    lanes with one shuffle, scaled by alpha/beta and scatter-written to C.
+//  1. Loader warps bring raw complex tiles into a ring of shared-memory
+//     stages.  A tile whose block-scatter blocks are regular (one uniform
+//     stride per bundle, the other unit stride) is fetched by ONE TMA
+//     instruction per operand (cp.async.bulk.tensor, 128-byte swizzle where
+//     the innermost run is K); other tiles are gathered element by element
+//     with cp.async through the scatter vectors (zero fill past the edges).
+//  2. Converter warps read a raw stage, build the 1M A rows [re, -im, ...]
+//     and [im, re, ...] for every complex row, split every value into TF32
+//     hi and lo parts (hi = rna(x), lo = rna(x - hi)) and store A hi/lo into
+//     TENSOR MEMORY with tcgen05.st (the 4x-expanded A never exists in shared
+//     or global memory) and B hi/lo into shared memory in the 128-byte-
+//     swizzled K-major layout the MMA descriptors read (the 1M B panel is the
+//     raw interleaved re/im data along K).
+//  3. One thread issues tcgen05.mma kind::tf32 (M = 128 real rows = 64 complex
+//     rows, N = 128 complex columns, K = 8).
 //
-// Pipelining: kStages stages of (A hi/lo in TMEM, B hi/lo in shared memory),
-// full/empty mbarriers between the 256 producer threads and the MMA thread;
-// tcgen05.commit releases a stage when its MMAs have read it.  Every wait is
-// bounded (ptx::mbar_wait); a timeout records an error code and the kernel
-// leaves after freeing its tensor memory.
+// Accuracy.  The tensor core's FP32 accumulation truncates: measured on
+// GB300, every MMA instruction that accumulates into D adds a bias of about
+// 2e-8 |D|, so 3 x 1024 MMAs over K = 4096 complex would cost ~6e-5 relative
+// error.  Therefore
+//  * the main product A_hi*B_hi goes into a short-lived CHUNK accumulator
+//    (two of them, ping-pong), restarted every kFold stages (128 real K =
+//    16 MMAs), and each finished chunk is folded by the converter warps into
+//    FP32 registers with round-to-nearest adds (tcgen05.ld + FADD);
+//  * the two correction products A_hi*B_lo + A_lo*B_hi (2^-11 of the main
+//    term) accumulate in a separate TMEM accumulator for the whole K range
+//    and are added once at the end.
+//  The epilogue pairs real rows 2i / 2i+1 (re / im of complex row i,
+//  t1m.h:425-426) across neighbouring lanes with one shuffle, applies
+//  alpha/beta and scatter-writes C.
+//
+// Synchronisation: mbarriers between loaders -> converters (raw ring),
+// converters -> MMA (operand stages), MMA -> converters (tcgen05.commit on
+// stage release and chunk completion).  Every wait is bounded
+// (ptx::mbar_wait); a timeout records an error code in a device word the
+// host checks, and the kernel leaves after freeing its tensor memory.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
+#include <mutex>
 #include <string>
 
 #include "internal.h"
@@ -42,36 +61,67 @@ namespace gb300 {
 namespace {
 
 constexpr int kTileMc = 64;     // complex rows per CTA (MMA M = 128 real rows)
-constexpr int kTileN = 256;     // complex columns per CTA (MMA N)
+constexpr int kTileN = 128;     // complex columns per CTA (MMA N)
 constexpr int kStepK = 16;      // complex K per stage = 32 TF32 = one 128 B swizzle row
-constexpr int kStages = 3;
-constexpr int kThreads = 384;   // warp 0: MMA + TMEM owner; warps 4..11: producers
-constexpr int kProducerBase = 128;
-constexpr int kProducers = 256;
+constexpr int kRaw = 4;         // raw tile stages
+constexpr int kStages = 2;      // converted operand stages
+constexpr int kFold = 4;        // stages per chunk accumulator (128 real K)
+constexpr int kThreads = 384;   // warp 0: MMA; warps 1-3: loaders; 4-11: converters
+constexpr int kLoaderBase = 32;
+constexpr int kLoaders = 96;
+constexpr int kConvBase = 128;
+constexpr int kConverters = 256;
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kAccCol = 0;      // accumulator: columns [0, 256)
-constexpr uint32_t kAStageCol = 256; // A stage s: columns 256 + 64 s (hi 32 | lo 32)
-constexpr int kBHalfBytes = kTileN * 128;       // 256 rows x 128 B
-constexpr int kStageBytes = 2 * kBHalfBytes;    // hi + lo
+constexpr uint32_t kChunkCol0 = 0;    // chunk accumulator 0: [0, 128)
+constexpr uint32_t kChunkCol1 = 128;  // chunk accumulator 1: [128, 256)
+constexpr uint32_t kCorrCol = 256;    // correction accumulator: [256, 384)
+constexpr uint32_t kAStageCol = 384;  // A stage s: 384 + 64 s (hi 32 | lo 32)
+
+constexpr int kRawABytes = kTileMc * kStepK * 8;   // 8 KB
+constexpr int kRawBBytes = kTileN * kStepK * 8;    // 16 KB
+constexpr int kRawBytes = kRawABytes + kRawBBytes;
+constexpr int kBHalfBytes = kTileN * 128;          // B hi (or lo): 128 rows x 128 B
+constexpr int kOpBytes = 2 * kBHalfBytes;
 constexpr int kBarrierBytes = 256;
-constexpr int kSmemBytes = 1024 + kStages * kStageBytes + kBarrierBytes;
+constexpr int kSmemBytes = 1024 + kRaw * kRawBytes + kStages * kOpBytes + kBarrierBytes;
 constexpr uint32_t kIdesc = ptx::idesc_f32acc(2u /*TF32*/, 128, kTileN);
 
 static_assert(kAStageCol + 64 * kStages <= kTmemCols, "TMEM budget");
 static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
+static_assert(kRawABytes % 1024 == 0 && kRawBBytes % 1024 == 0, "TMA swizzle alignment");
 
-enum : int { kErrFullWait = 1, kErrEmptyWait = 2, kErrAccWait = 3 };
+enum : int {
+  kErrFullWait = 1,
+  kErrEmptyWait = 2,
+  kErrAccWait = 3,
+  kErrChunkWait = 4,
+  kErrRawWait = 5
+};
+
+// How a raw operand tile is fetched, and hence its shared-memory layout.
+//   A: kMK  [k][m]   512 B per k, TMA (M unit stride)       / gather
+//      kKM  [m][k]   128 B rows, 128 B swizzle, TMA (K unit stride)
+//   B: kNK  [n][k]   128 B rows, 128 B swizzle, TMA (K unit stride) / gather
+//      kKN  [k][n]   1024 B per k, TMA (N unit stride)
+enum : int { kTmaMK = 0, kTmaKM = 1, kGatherMK = 2 };
+enum : int { kTmaNK = 0, kTmaKN = 1, kGatherNK = 2 };
+
+struct TmaMaps {
+  CUtensorMap a;
+  CUtensorMap b;
+};
 
 __device__ __forceinline__ int64_t offs(const int64_t* v, int64_t u, int64_t i) {
   return u >= 0 ? i * u : __ldg(v + i);
 }
 
-__device__ __forceinline__ uint32_t swz128(int n, int k) {
-  // Byte offset of complex element (row n, complex k) in a 128 B-swizzled
-  // K-major tile of TF32 pairs: 16-byte chunk (k/2) of row n lands at chunk
-  // (k/2) ^ (n % 8) of its 128-byte row; rows grouped in 1024-byte atoms.
-  return static_cast<uint32_t>((n >> 3) * 1024 + (n & 7) * 128 +
-                               ((((k >> 1) ^ (n & 7)) & 7) << 4) + (k & 1) * 8);
+// Byte offset of complex element (row r, complex k) in a 128 B-swizzled tile
+// of 128-byte rows: 16-byte chunk (k/2) of row r lands at chunk (k/2)^(r%8);
+// rows are grouped in 1024-byte atoms.  This is both the TMA SWIZZLE_128B
+// layout and the UMMA K-major SW128 layout.
+__device__ __forceinline__ uint32_t swz128(int r, int k) {
+  return static_cast<uint32_t>((r >> 3) * 1024 + (r & 7) * 128 +
+                               ((((k >> 1) ^ (r & 7)) & 7) << 4) + (k & 1) * 8);
 }
 
 __device__ __forceinline__ void record_error(int* flag, int code) {
@@ -88,19 +138,56 @@ __device__ __forceinline__ Split split_tf32(float x) {
   return {__float_as_uint(h), __float_as_uint(l)};
 }
 
+__device__ __forceinline__ float2 lds64(uint32_t addr) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ float4 lds128(uint32_t addr) {
+  float4 v;
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "r"(addr));
+  return v;
+}
+__device__ __forceinline__ void sts64(uint32_t addr, uint32_t a, uint32_t b) {
+  asm volatile("st.shared.v2.b32 [%0], {%1, %2};" ::"r"(addr), "r"(a), "r"(b) : "memory");
+}
+__device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, uint32_t c,
+                                       uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c),
+               "r"(d)
+               : "memory");
+}
+
+template <int AMode, int BMode>
 __global__ void __launch_bounds__(kThreads, 1)
-tc3xtf32_contract(const GemmArgs args, int* err_flag, int b_kcontig) {
+tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
+  constexpr bool kTmaA = AMode != kGatherMK;
+  constexpr bool kTmaB = BMode != kGatherNK;
+  constexpr bool kGather = !kTmaA || !kTmaB;
+  // Arrivals per raw stage: one expect_tx arrive from the TMA thread, one
+  // cp.async completion arrive per gather thread.
+  constexpr uint32_t kRawArrivals = (kTmaA || kTmaB ? 1u : 0u) + (kGather ? kLoaders : 0u);
+  constexpr uint32_t kTmaBytes = (kTmaA ? kRawABytes : 0) + (kTmaB ? kRawBBytes : 0);
+
   extern __shared__ __align__(16) uint8_t smem_raw[];
-  const uint32_t raw = ptx::smem_u32(smem_raw);
-  const uint32_t sb = (raw + 1023u) & ~1023u;            // B stages (1024-aligned)
-  uint8_t* const sb_ptr = smem_raw + (sb - raw);
-  const uint32_t bars = sb + kStages * kStageBytes;
-  auto full_bar = [&](int s) { return bars + 8u * s; };
-  auto empty_bar = [&](int s) { return bars + 8u * (kStages + s); };
-  const uint32_t acc_bar = bars + 16u * kStages;
+  const uint32_t base = (ptx::smem_u32(smem_raw) + 1023u) & ~1023u;
+  uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
+  const uint32_t raw0 = base;                          // kRaw x (A 8 KB | B 16 KB)
+  const uint32_t op0 = raw0 + kRaw * kRawBytes;        // kStages x (B hi | B lo)
+  const uint32_t bars = op0 + kStages * kOpBytes;
+  auto raw_a = [&](int r) { return raw0 + r * kRawBytes; };
+  auto raw_b = [&](int r) { return raw0 + r * kRawBytes + kRawABytes; };
+  auto raw_full = [&](int r) { return bars + 8u * r; };
+  auto raw_empty = [&](int r) { return bars + 8u * (kRaw + r); };
+  auto full_bar = [&](int s) { return bars + 8u * (2 * kRaw + s); };
+  auto empty_bar = [&](int s) { return bars + 8u * (2 * kRaw + kStages + s); };
+  auto chunk_full = [&](int b) { return bars + 8u * (2 * kRaw + 2 * kStages + b); };
+  auto chunk_empty = [&](int b) { return bars + 8u * (2 * kRaw + 2 * kStages + 2 + b); };
+  const uint32_t acc_bar = bars + 8u * (2 * kRaw + 2 * kStages + 4);
   const uint32_t tmem_slot = acc_bar + 8u;
-  volatile uint32_t* tmem_slot_ptr =
-      reinterpret_cast<volatile uint32_t*>(sb_ptr + kStages * kStageBytes + 16 * kStages + 8);
+  volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(base_ptr + (tmem_slot - base));
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
@@ -110,12 +197,24 @@ tc3xtf32_contract(const GemmArgs args, int* err_flag, int b_kcontig) {
     ptx::tmem_relinquish();
   }
   if (tid == 32) {
+    for (int r = 0; r < kRaw; ++r) {
+      ptx::mbar_init(raw_full(r), kRawArrivals);
+      ptx::mbar_init(raw_empty(r), kConverters / 32);
+    }
     for (int s = 0; s < kStages; ++s) {
-      ptx::mbar_init(full_bar(s), kProducers / 32);
+      ptx::mbar_init(full_bar(s), kConverters / 32);
       ptx::mbar_init(empty_bar(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(chunk_full(b), 1);
+      ptx::mbar_init(chunk_empty(b), kConverters / 32);
     }
     ptx::mbar_init(acc_bar, 1);
     ptx::fence_mbar_init();
+  }
+  if (tid == 64) {
+    if (kTmaA) ptx::tma_prefetch_desc(&maps.a);
+    if (kTmaB) ptx::tma_prefetch_desc(&maps.b);
   }
   ptx::tc_fence_before();
   __syncthreads();
@@ -139,30 +238,38 @@ tc3xtf32_contract(const GemmArgs args, int* err_flag, int b_kcontig) {
   if (warp == 0) {
     // ---------------------------------------------------------- MMA issue ---
     if (lane == 0) {
-      bool ok = true;
-      for (int64_t s = 0; s < ksteps && ok; ++s) {
+      for (int64_t s = 0; s < ksteps; ++s) {
         const int st = static_cast<int>(s % kStages);
         const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
+        const int64_t c = s / kFold;
+        const int buf = static_cast<int>(c & 1);
+        const bool chunk_start = (s % kFold) == 0;
+        if (chunk_start && c >= 2 &&
+            !ptx::mbar_wait(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
+          record_error(err_flag, kErrChunkWait);
+          break;
+        }
         if (!ptx::mbar_wait(full_bar(st), ph)) {
           record_error(err_flag, kErrFullWait);
-          ok = false;
           break;
         }
         ptx::tc_fence_after();
+        const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
+        const uint32_t d_corr = tmem + kCorrCol;
         const uint32_t a_hi = tmem + kAStageCol + 64u * st;
         const uint32_t a_lo = a_hi + 32u;
-        const uint32_t b_hi = sb + st * kStageBytes;
+        const uint32_t b_hi = op0 + st * kOpBytes;
         const uint32_t b_lo = b_hi + kBHalfBytes;
 #pragma unroll
         for (int kk = 0; kk < 4; ++kk) {
           const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
           const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
-          const uint32_t first = (s == 0 && kk == 0) ? 0u : 1u;
-          ptx::mma_tf32_ts(tmem + kAccCol, a_hi + 8u * kk, dh, kIdesc, first);
-          ptx::mma_tf32_ts(tmem + kAccCol, a_hi + 8u * kk, dl, kIdesc, 1u);
-          ptx::mma_tf32_ts(tmem + kAccCol, a_lo + 8u * kk, dh, kIdesc, 1u);
+          ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
+          ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
+          ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
         }
         ptx::mma_commit(empty_bar(st));
+        if ((s % kFold) == kFold - 1 || s == ksteps - 1) ptx::mma_commit(chunk_full(buf));
       }
       // Signal the epilogue (also after an abort, so nobody waits forever),
       // then make sure no MMA is still writing TMEM before it is freed.
@@ -170,68 +277,131 @@ tc3xtf32_contract(const GemmArgs args, int* err_flag, int b_kcontig) {
       if (!ptx::mbar_wait(acc_bar, 0)) record_error(err_flag, kErrAccWait);
     }
     __syncwarp();
-  } else if (tid >= kProducerBase) {
-    // ---------------------------------------------------------- producers ---
-    const int pt = tid - kProducerBase;
-    const int wg = pt >> 7;          // which half of the K-step (A) / of N (B)
+  } else if (tid < kConvBase) {
+    // ------------------------------------------------------------ loaders ---
+    const int lt = tid - kLoaderBase;  // 0..95
+    const float2* __restrict__ A = static_cast<const float2*>(args.A);
+    const float2* __restrict__ B = static_cast<const float2*>(args.B);
+    // Gather work of this thread: fixed rows / columns, K walked per stage.
+    for (int64_t s = 0; s < ksteps; ++s) {
+      const int r = static_cast<int>(s % kRaw);
+      const uint32_t ph = static_cast<uint32_t>((s / kRaw) & 1);
+      const int64_t k0 = s * kStepK;
+      if (kGather || lt == 0) {
+        if (!ptx::mbar_wait(raw_empty(r), ph ^ 1u)) {
+          record_error(err_flag, kErrRawWait);
+          break;
+        }
+      }
+      if ((kTmaA || kTmaB) && lt == 0) {
+        ptx::mbar_arrive_expect_tx(raw_full(r), kTmaBytes);
+        if (AMode == kTmaMK)
+          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * m0), static_cast<int>(k0), raw_full(r));
+        if (AMode == kTmaKM)
+          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * k0), static_cast<int>(m0), raw_full(r));
+        if (BMode == kTmaNK)
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * k0), static_cast<int>(n0), raw_full(r));
+        if (BMode == kTmaKN)
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * n0), static_cast<int>(k0), raw_full(r));
+      }
+      if (kGather) {
+        if (AMode == kGatherMK) {
+          // [k][m]: consecutive threads walk m (coalesced where M is unit stride).
+          for (int e = lt; e < kTileMc * kStepK; e += kLoaders) {
+            const int m = e % kTileMc, k = e / kTileMc;
+            const bool ok = (m0 + m < M) && (k0 + k < K);
+            const float2* src = ok ? A + offs(args.rsA, args.uA_m, m0 + m) + offs(args.csA, args.uA_k, k0 + k) : A;
+            ptx::cp_async_8(raw_a(r) + static_cast<uint32_t>(k * 512 + m * 8), src, ok ? 8u : 0u);
+          }
+        }
+        if (BMode == kGatherNK) {
+          // [n][k] swizzled: consecutive threads walk k.
+          for (int e = lt; e < kTileN * kStepK; e += kLoaders) {
+            const int k = e % kStepK, n = e / kStepK;
+            const bool ok = (n0 + n < N) && (k0 + k < K);
+            const float2* src = ok ? B + offs(args.rsB, args.uB_k, k0 + k) + offs(args.csB, args.uB_n, n0 + n) : B;
+            ptx::cp_async_8(raw_b(r) + swz128(n, k), src, ok ? 8u : 0u);
+          }
+        }
+        ptx::cp_async_arrive_noinc(raw_full(r));
+      }
+    }
+  } else {
+    // -------------------------------------------- converters, fold, epilogue ---
+    const int pt = tid - kConvBase;
+    const int wg = pt >> 7;          // which half of the K-step (A) / of N (B, C)
     const int q = (pt >> 5) & 3;     // TMEM lane quarter of this warp
     const int rho = 32 * q + lane;   // real row = TMEM lane
     const int ci = rho >> 1;         // complex row in the tile
     const int part = rho & 1;        // 0: real row "re", 1: "im"
+    const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
     const bool conjA = args.flags & kFlagConjA;
     const bool conjB = args.flags & kFlagConjB;
-    const float2* __restrict__ A = static_cast<const float2*>(args.A);
-    const float2* __restrict__ B = static_cast<const float2*>(args.B);
-
     const bool row_ok = (m0 + ci) < M;
-    const int64_t rowA = row_ok ? offs(args.rsA, args.uA_m, m0 + ci) : 0;
-    const int tw = pt & 127;
-    // B element (n, k) handled in slot j: K-contiguous tensors walk k across
-    // neighbouring threads (coalesced 128-byte column runs), others walk n.
-    auto b_n = [&](int j) { return b_kcontig ? (wg * 128 + (tw >> 4) + 8 * j) : (wg * 128 + tw); };
-    auto b_k = [&](int j) { return b_kcontig ? (tw & 15) : j; };
 
-    float2 va[4], vb[16];
-    auto load = [&](int64_t k0) {
+    float master[64];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int64_t kk = k0 + wg * 8 + 2 * j + part;
-        float2 v = make_float2(0.f, 0.f);
-        if (row_ok && kk < K) v = A[rowA + offs(args.csA, args.uA_k, kk)];
-        if (conjA) v.y = -v.y;
-        va[j] = v;
-      }
+    for (int j = 0; j < 64; ++j) master[j] = 0.f;
+
+    // Fold chunk accumulator at column `col` into the FP32 master registers
+    // (round-to-nearest adds): this thread's lane, 64 columns.
+    auto fold_from = [&](uint32_t col) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int64_t n = n0 + b_n(j);
-        const int64_t kk = k0 + b_k(j);
-        float2 v = make_float2(0.f, 0.f);
-        if (n < N && kk < K) v = B[offs(args.rsB, args.uB_k, kk) + offs(args.csB, args.uB_n, n)];
-        if (conjB) v.y = -v.y;
-        vb[j] = v;
+      for (int cc = 0; cc < 4; ++cc) {
+        uint32_t r[16];
+        ptx::tmem_ld16(tmem + lane_base + col + 64u * wg + 16u * cc, r);
+        ptx::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) master[16 * cc + j] += __uint_as_float(r[j]);
       }
     };
 
     bool ok = true;
-    load(0);
     for (int64_t s = 0; s < ksteps; ++s) {
+      const int r = static_cast<int>(s % kRaw);
+      const uint32_t rph = static_cast<uint32_t>((s / kRaw) & 1);
       const int st = static_cast<int>(s % kStages);
       const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
-      // A row values for this half of the step: the pair (2i, 2i+1) loaded
-      // alternate k; exchange so both hold all eight.
+
+      if (!ptx::mbar_wait(raw_full(r), rph)) {
+        record_error(err_flag, kErrRawWait);
+        ok = false;
+        break;
+      }
+      // A: eight complex k (this half of the step) of complex row ci.
       float2 av[8];
+      if (AMode == kTmaKM) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float4 v = lds128(raw_a(r) + swz128(ci, 8 * wg + 2 * j));
+          av[2 * j] = make_float2(v.x, v.y);
+          av[2 * j + 1] = make_float2(v.z, v.w);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) av[j] = lds64(raw_a(r) + static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8));
+      }
+      // B: four 16-byte pieces (two complex each) of the raw tile.
+      float4 bv[4];
+      uint32_t boff[4][2];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        float2 other;
-        other.x = __shfl_xor_sync(0xffffffffu, va[j].x, 1);
-        other.y = __shfl_xor_sync(0xffffffffu, va[j].y, 1);
-        av[2 * j] = part ? other : va[j];
-        av[2 * j + 1] = part ? va[j] : other;
+        const int id = pt + 256 * j;
+        if (BMode == kTmaKN) {
+          const int k = id >> 6, n = 2 * (id & 63);
+          bv[j] = lds128(raw_b(r) + static_cast<uint32_t>(k * 1024 + n * 8));
+          boff[j][0] = swz128(n, k);
+          boff[j][1] = swz128(n + 1, k);
+        } else {
+          const int n = id >> 3, kp = id & 7;
+          const uint32_t off = swz128(n, 2 * kp);
+          bv[j] = lds128(raw_b(r) + off);
+          boff[j][0] = off;
+          boff[j][1] = 0;
+        }
       }
-      float2 bv[16];
-#pragma unroll
-      for (int j = 0; j < 16; ++j) bv[j] = vb[j];
-      if (s + 1 < ksteps) load((s + 1) * kStepK);  // prefetch the next step
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(raw_empty(r));
 
       if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
         record_error(err_flag, kErrEmptyWait);
@@ -243,31 +413,62 @@ tc3xtf32_contract(const GemmArgs args, int* err_flag, int b_kcontig) {
       uint32_t hi[16], lo[16];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        const float x0 = part ? av[j].y : av[j].x;
-        const float x1 = part ? av[j].x : -av[j].y;
+        float2 v = av[j];
+        if (conjA) v.y = -v.y;
+        if (!row_ok) v = make_float2(0.f, 0.f);
+        const float x0 = part ? v.y : v.x;
+        const float x1 = part ? v.x : -v.y;
         const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
         hi[2 * j] = s0.hi;
         lo[2 * j] = s0.lo;
         hi[2 * j + 1] = s1.hi;
         lo[2 * j + 1] = s1.lo;
       }
-      const uint32_t a_col = tmem + (static_cast<uint32_t>(32 * q) << 16) + kAStageCol + 64u * st + 16u * wg;
+      const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 16u * wg;
       ptx::tmem_st16(a_col, hi);
       ptx::tmem_st16(a_col + 32u, lo);
       // B -> shared memory (swizzled K-major hi and lo tiles).
-      uint8_t* bst = sb_ptr + st * kStageBytes;
+      const uint32_t ob = op0 + st * kOpBytes;
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const Split r = split_tf32(bv[j].x), im = split_tf32(bv[j].y);
-        const uint32_t off = swz128(b_n(j), b_k(j));
-        *reinterpret_cast<uint2*>(bst + off) = make_uint2(r.hi, im.hi);
-        *reinterpret_cast<uint2*>(bst + kBHalfBytes + off) = make_uint2(r.lo, im.lo);
+      for (int j = 0; j < 4; ++j) {
+        float4 v = bv[j];
+        if (conjB) {
+          v.y = -v.y;
+          v.w = -v.w;
+        }
+        const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
+        const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
+        if (BMode == kTmaKN) {
+          sts64(ob + boff[j][0], r0.hi, i0.hi);
+          sts64(ob + boff[j][1], r1.hi, i1.hi);
+          sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
+          sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
+        } else {
+          sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
+          sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+        }
       }
       ptx::tmem_wait_st();
       ptx::fence_proxy_async_smem();
       ptx::tc_fence_before();
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(full_bar(st));
+
+      // Fold the previous chunk once the first stage of the next is queued.
+      if ((s % kFold) == 0 && s >= kFold) {
+        const int64_t c = s / kFold - 1;
+        const int buf = static_cast<int>(c & 1);
+        if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
+          record_error(err_flag, kErrChunkWait);
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        fold_from(buf ? kChunkCol1 : kChunkCol0);
+        ptx::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(chunk_empty(buf));
+      }
     }
 
     // ---------------------------------------------------------- epilogue ---
@@ -277,41 +478,37 @@ tc3xtf32_contract(const GemmArgs args, int* err_flag, int b_kcontig) {
     }
     ptx::tc_fence_after();
     if (ok) {
+      // The last chunk was never folded in the loop; then add the corrections.
+      const int64_t c_last = (ksteps - 1) / kFold;
+      fold_from((c_last & 1) ? kChunkCol1 : kChunkCol0);
+      fold_from(kCorrCol);
       const bool accumulate = args.flags & kFlagAccumulate;
       const bool beta_zero = args.flags & kFlagBetaZero;
       const float ar = (float)args.alpha[0], ai = (float)args.alpha[1];
       const float br = (float)args.beta[0], bi = (float)args.beta[1];
       float2* __restrict__ Cp = static_cast<float2*>(args.C);
       const int64_t rowC = row_ok ? offs(args.rsC, args.uC_m, m0 + ci) : 0;
-#pragma unroll 1
-      for (int cc = 0; cc < 8; ++cc) {
-        const int c0 = wg * 128 + 16 * cc;
-        uint32_t r[16];
-        ptx::tmem_ld16(tmem + (static_cast<uint32_t>(32 * q) << 16) + kAccCol + c0, r);
-        ptx::tmem_wait_ld();
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-          const float va0 = __uint_as_float(r[2 * j]);
-          const float va1 = __uint_as_float(r[2 * j + 1]);
-          const float send = part ? va0 : va1;
-          const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-          const int col = c0 + 2 * j + part;
-          const float re = part ? recv : va0;
-          const float im = part ? va1 : recv;
-          const int64_t n = n0 + col;
-          if (row_ok && n < N) {
-            float2* p = Cp + rowC + offs(args.csC, args.uC_n, n);
-            const float tr = ar * re - ai * im;
-            const float ti = ar * im + ai * re;
-            if (accumulate) {
-              const float2 o = *p;
-              *p = make_float2(o.x + tr, o.y + ti);
-            } else if (beta_zero) {
-              *p = make_float2(tr, ti);
-            } else {
-              const float2 o = *p;
-              *p = make_float2(tr + (br * o.x - bi * o.y), ti + (br * o.y + bi * o.x));
-            }
+      for (int j = 0; j < 32; ++j) {
+        const float v0 = master[2 * j], v1 = master[2 * j + 1];
+        const float send = part ? v0 : v1;
+        const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+        const int col = wg * 64 + 2 * j + part;
+        const float re = part ? recv : v0;
+        const float im = part ? v1 : recv;
+        const int64_t n = n0 + col;
+        if (row_ok && n < N) {
+          float2* p = Cp + rowC + offs(args.csC, args.uC_n, n);
+          const float tr = ar * re - ai * im;
+          const float ti = ar * im + ai * re;
+          if (accumulate) {
+            const float2 o = *p;
+            *p = make_float2(o.x + tr, o.y + ti);
+          } else if (beta_zero) {
+            *p = make_float2(tr, ti);
+          } else {
+            const float2 o = *p;
+            *p = make_float2(tr + (br * o.x - bi * o.y), ti + (br * o.y + bi * o.x));
           }
         }
       }
@@ -326,7 +523,69 @@ tc3xtf32_contract(const GemmArgs args, int* err_flag, int b_kcontig) {
   }
 }
 
-bool g_attr_set = false;
+// ------------------------------------------------------------------ host ---
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  });
+  return fn;
+}
+
+// 2-D map over a complex64 matrix viewed as floats: dim0 = 2*inner (unit
+// stride), dim1 = outer with `outer_stride` complex elements.
+bool make_map(CUtensorMap* map, const void* base, int64_t inner, int64_t outer,
+              int64_t outer_stride, uint32_t box_inner_floats, uint32_t box_outer, bool swizzle) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  if (outer > 1 && ((outer_stride * 8) % 16 != 0 || outer_stride <= 0)) return false;
+  if (2 * inner >= (int64_t(1) << 31) || outer >= (int64_t(1) << 31)) return false;
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(2 * inner), static_cast<cuuint64_t>(outer)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(outer > 1 ? outer_stride * 8 : 16)};
+  cuuint32_t box[2] = {box_inner_floats, box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+template <int AMode, int BMode>
+cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
+                         int* err_flag, unsigned tiles) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc3xtf32_contract<AMode, BMode>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  tc3xtf32_contract<AMode, BMode><<<tiles, kThreads, kSmemBytes, stream>>>(args, maps, err_flag);
+  return cudaGetLastError();
+}
+
+template <int AMode>
+cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
+                     int* err_flag, unsigned tiles) {
+  switch (bmode) {
+    case kTmaNK: return launch_modes<AMode, kTmaNK>(args, maps, stream, err_flag, tiles);
+    case kTmaKN: return launch_modes<AMode, kTmaKN>(args, maps, stream, err_flag, tiles);
+    default: return launch_modes<AMode, kGatherNK>(args, maps, stream, err_flag, tiles);
+  }
+}
 
 }  // namespace
 
@@ -342,19 +601,35 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     *err = "tensor-core method not available for this dtype";
     return cudaErrorNotSupported;
   }
-  if (!g_attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc3xtf32_contract,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    if (e != cudaSuccess) return e;
-    g_attr_set = true;
-  }
   const int64_t tiles = ((args.M + kTileMc - 1) / kTileMc) * ((args.N + kTileN - 1) / kTileN);
   if (tiles == 0) return cudaSuccess;
-  const int b_kcontig = (plan.uB_k == 1) ? 1 : 0;
-  tc3xtf32_contract<<<static_cast<unsigned>(tiles), kThreads, kSmemBytes, stream>>>(
-      args, err_flag, b_kcontig);
-  *kernels = 1;
-  return cudaGetLastError();
+  if (tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  // Operand fetch modes: TMA where the matricised operand is a regular 2-D
+  // strided matrix with one unit-stride direction, gather otherwise.
+  TmaMaps maps;
+  std::memset(&maps, 0, sizeof(maps));
+  int amode = kGatherMK, bmode = kGatherNK;
+  if (plan.uA_m == 1 && plan.uA_k >= 0 &&
+      make_map(&maps.a, args.A, args.M, args.K, plan.uA_k, 2 * kTileMc, kStepK, false))
+    amode = kTmaMK;
+  else if (plan.uA_k == 1 && plan.uA_m >= 0 &&
+           make_map(&maps.a, args.A, args.K, args.M, plan.uA_m, 2 * kStepK, kTileMc, true))
+    amode = kTmaKM;
+  if (plan.uB_k == 1 && plan.uB_n >= 0 &&
+      make_map(&maps.b, args.B, args.K, args.N, plan.uB_n, 2 * kStepK, kTileN, true))
+    bmode = kTmaNK;
+  else if (plan.uB_n == 1 && plan.uB_k >= 0 &&
+           make_map(&maps.b, args.B, args.N, args.K, plan.uB_k, 2 * kTileN, kStepK, false))
+    bmode = kTmaKN;
+  cudaError_t e;
+  const unsigned nt = static_cast<unsigned>(tiles);
+  switch (amode) {
+    case kTmaMK: e = launch_b<kTmaMK>(bmode, args, maps, stream, err_flag, nt); break;
+    case kTmaKM: e = launch_b<kTmaKM>(bmode, args, maps, stream, err_flag, nt); break;
+    default: e = launch_b<kGatherMK>(bmode, args, maps, stream, err_flag, nt); break;
+  }
+  if (e == cudaSuccess) *kernels = 1;
+  return e;
 }
 
 }  // namespace gb300
