@@ -92,7 +92,7 @@ constexpr int kThreads = 256;
 // and columns tx + 16*j (j < TN), so shared-memory reads of B are
 // consecutive across a half-warp and reads of A are broadcasts.
 template <class T, int TM, int TN, int BK>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
 simt_contract(const GemmArgs args) {
   constexpr int BM = 16 * TM;
   constexpr int BN = 16 * TN;
@@ -101,8 +101,11 @@ simt_contract(const GemmArgs args) {
   static_assert(A_PER * kThreads == BM * BK, "A tile not divisible");
   static_assert(B_PER * kThreads == BN * BK, "B tile not divisible");
 
-  __shared__ T As[2][BK][BM];
-  __shared__ T Bs[2][BK][BN];
+  // Rows padded by 32 bytes: tile stores that walk k across threads (a
+  // K-contiguous operand) then spread over the banks instead of hitting one.
+  constexpr int kPad = 32 / sizeof(T);
+  __shared__ __align__(16) T As[2][BK][BM + kPad];
+  __shared__ __align__(16) T Bs[2][BK][BN + kPad];
   __shared__ int64_t rowA[BM];
   __shared__ int64_t colB[BN];
 

@@ -132,9 +132,16 @@ struct Split {
   uint32_t hi, lo;
 };
 
+// hi/lo split on the FMA pipe (Veltkamp splitting, factor 2^13 + 1): hi keeps
+// the leading 11 significant bits of x rounded to nearest (exactly a TF32
+// value), lo = x - hi is exact with at most 13 significant bits, of which the
+// TF32 MMA uses the leading 11 (|error| <= 2^-22 |x|).  Valid for
+// |x| < 2^127 / 8193; the _rn intrinsics keep the compiler from contracting
+// or reassociating the three operations.
 __device__ __forceinline__ Split split_tf32(float x) {
-  const float h = ptx::tf32_rna(x);
-  const float l = ptx::tf32_rna(x - h);
+  const float c = __fmul_rn(x, 8193.0f);
+  const float h = __fsub_rn(c, __fsub_rn(c, x));
+  const float l = __fsub_rn(x, h);
   return {__float_as_uint(h), __float_as_uint(l)};
 }
 
@@ -356,50 +363,57 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
       }
     };
 
-    bool ok = true;
-    for (int64_t s = 0; s < ksteps; ++s) {
-      const int r = static_cast<int>(s % kRaw);
-      const uint32_t rph = static_cast<uint32_t>((s / kRaw) & 1);
-      const int st = static_cast<int>(s % kStages);
-      const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
+    // Loop-invariant shared-memory offsets of this thread's raw reads and
+    // operand writes.
+    uint32_t aoff[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      aoff[j] = (AMode == kTmaKM) ? swz128(ci, 8 * wg + 2 * (j >> 1))
+                                  : static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8);
+    uint32_t bsrc[4], boff[4][2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int id = pt + 256 * j;
+      if (BMode == kTmaKN) {
+        const int k = id >> 6, n = 2 * (id & 63);
+        bsrc[j] = static_cast<uint32_t>(k * 1024 + n * 8);
+        boff[j][0] = swz128(n, k);
+        boff[j][1] = swz128(n + 1, k);
+      } else {
+        const int n = id >> 3, kp = id & 7;
+        bsrc[j] = swz128(n, 2 * kp);
+        boff[j][0] = bsrc[j];
+        boff[j][1] = 0;
+      }
+    }
 
+    bool ok = true;
+    int r = 0, st = 0;
+    uint32_t rph = 0, ph = 0;
+    for (int64_t s = 0; s < ksteps; ++s) {
       if (!ptx::mbar_wait(raw_full(r), rph)) {
         record_error(err_flag, kErrRawWait);
         ok = false;
         break;
       }
       // A: eight complex k (this half of the step) of complex row ci.
+      const uint32_t ra = raw_a(r), rb = raw_b(r);
       float2 av[8];
       if (AMode == kTmaKM) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const float4 v = lds128(raw_a(r) + swz128(ci, 8 * wg + 2 * j));
+          const float4 v = lds128(ra + aoff[2 * j]);
           av[2 * j] = make_float2(v.x, v.y);
           av[2 * j + 1] = make_float2(v.z, v.w);
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) av[j] = lds64(raw_a(r) + static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8));
+        for (int j = 0; j < 8; ++j) av[j] = lds64(ra + aoff[j]);
       }
       // B: four 16-byte pieces (two complex each) of the raw tile.
       float4 bv[4];
-      uint32_t boff[4][2];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int id = pt + 256 * j;
-        if (BMode == kTmaKN) {
-          const int k = id >> 6, n = 2 * (id & 63);
-          bv[j] = lds128(raw_b(r) + static_cast<uint32_t>(k * 1024 + n * 8));
-          boff[j][0] = swz128(n, k);
-          boff[j][1] = swz128(n + 1, k);
-        } else {
-          const int n = id >> 3, kp = id & 7;
-          const uint32_t off = swz128(n, 2 * kp);
-          bv[j] = lds128(raw_b(r) + off);
-          boff[j][0] = off;
-          boff[j][1] = 0;
-        }
-      }
+      for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(raw_empty(r));
 
@@ -468,6 +482,14 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
         ptx::tc_fence_before();
         __syncwarp();
         if (lane == 0) ptx::mbar_arrive(chunk_empty(buf));
+      }
+      if (++r == kRaw) {
+        r = 0;
+        rph ^= 1u;
+      }
+      if (++st == kStages) {
+        st = 0;
+        ph ^= 1u;
       }
     }
 
