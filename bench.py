@@ -57,6 +57,18 @@ def _peaks() -> dict:
             "sm_max_mhz": 2070.0, "_source": "fallback"}
 
 
+def _profiled_traffic():
+    """DRAM bytes (read + write) per launch of the tensor-core kernel on this
+    workload, from the committed ncu summary (None if absent)."""
+    p = ROOT / "profiles" / "tc3xtf32_ijkl_klmn_64.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch"):
+            return int(line.split("=")[1])
+    return None
+
+
 class ClockSampler:
     """nvidia-smi clocks/throttle sampling while the timed region runs."""
 
@@ -347,7 +359,10 @@ def run_gpu(args) -> None:
                         "oracle": "2048 sampled entries, FP64 dot products"},
             "roofline": {"bound": "tensor" if tc_method != "plain" else "fp32-simt",
                          "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",
-                         "frac": kernel_tflops / peak, "traffic": None,
+                         "frac": kernel_tflops / peak,
+                         "traffic": _profiled_traffic() if tc_method == "tc_3xtf32" else None,
+                         "traffic_source": "profiles/tc3xtf32_ijkl_klmn_64.md (ncu dram bytes "
+                                           "read+write per launch)",
                          "peak_note": peak_note},
             "e2e": {"value": world * FLOPS / e2e_s / 1e12, "unit": "TFLOP/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
