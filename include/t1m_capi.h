@@ -111,6 +111,11 @@ int t1m_destroy(t1m_context* ctx);
 /* Run on a caller-owned cudaStream_t (NULL = the context's own stream). */
 int t1m_set_stream(t1m_context* ctx, void* stream);
 int t1m_set_method(t1m_context* ctx, int method);
+/* Number of K partitions (split-K with an FP64 reduction of the partial
+ * products); 0 = automatic (split when the output has too few tiles to fill
+ * the GPU).  The reference streams K in KC chunks inside one thread
+ * (t1m.h:512-548); this is its parallel counterpart. */
+int t1m_set_split_k(t1m_context* ctx, int splits);
 int t1m_synchronize(t1m_context* ctx);
 const char* t1m_status_string(int status);
 const char* t1m_last_error(const t1m_context* ctx);

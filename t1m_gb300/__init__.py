@@ -111,6 +111,7 @@ def lib() -> C.CDLL:
         h.t1m_destroy.argtypes = [vp]
         h.t1m_set_stream.argtypes = [vp, vp]
         h.t1m_set_method.argtypes = [vp, i32]
+        h.t1m_set_split_k.argtypes = [vp, i32]
         h.t1m_synchronize.argtypes = [vp]
         h.t1m_status_string.restype = C.c_char_p
         h.t1m_status_string.argtypes = [i32]
@@ -140,6 +141,10 @@ class Context:
         if isinstance(m, str):
             m = method[m]
         self._check(lib().t1m_set_method(self._h, int(m)))
+
+    def set_split_k(self, splits: int) -> None:
+        """Force the number of K partitions (0 = automatic)."""
+        self._check(lib().t1m_set_split_k(self._h, int(splits)))
 
     def set_stream(self, stream: int | None) -> None:
         self._check(lib().t1m_set_stream(self._h, stream or None))

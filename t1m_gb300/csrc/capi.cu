@@ -9,6 +9,7 @@
 // a missing or failed kernel is an error, never a CPU fallback.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <list>
@@ -26,9 +27,10 @@ using namespace t1m::gb300;
 namespace t1m {
 namespace gb300 {
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args,
-                      const HostPlan& plan, cudaStream_t stream, int* err_flag,
-                      int* kernels, std::string* err);
+                      const HostPlan& plan, int splits, cudaStream_t stream,
+                      int* err_flag, int* kernels, std::string* err);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
+void tc_tile(int* bm, int* bn, int* bk);
 }  // namespace gb300
 }  // namespace t1m
 
@@ -52,6 +54,11 @@ struct t1m_context {
   // Staging buffers for host operands (grow only).
   void* stage[3] = {nullptr, nullptr, nullptr};
   size_t stage_bytes[3] = {0, 0, 0};
+  // Split-K workspace (grow only) and the forced split count (0 = automatic).
+  void* work = nullptr;
+  size_t work_bytes = 0;
+  int split_k = 0;
+  int num_sms = 152;
 };
 
 namespace {
@@ -178,9 +185,58 @@ int choose_method(const t1m_context* ctx, int dtype, const HostPlan& plan) {
   int m = ctx->method;
   if (m != T1M_METHOD_AUTO) return m;
   if (dtype == T1M_COMPLEX64 && tc_supported(T1M_METHOD_TC_3XTF32, dtype, plan) &&
-      plan.M * plan.N >= 128 * 256 && plan.K >= 64)
+      plan.M * plan.N * plan.K >= int64_t(1) << 18)
     return T1M_METHOD_TC_3XTF32;
   return T1M_METHOD_PLAIN;
+}
+
+// Workspace cap of split-K (bytes of partial products).
+constexpr size_t kMaxWorkBytes = size_t(2) << 30;
+
+// Number of K splits: enough CTAs for about one full wave when the output
+// has too few tiles, each split keeping at least four K-steps; forced by
+// t1m_set_split_k.  Returns the split count and its K length (a multiple of
+// the kernel's K-step).
+int choose_splits(const t1m_context* ctx, int method, int dtype, const HostPlan& hp,
+                  size_t elem, int64_t* k_per_split) {
+  int bm, bn, bk, per_sm;
+  if (method == T1M_METHOD_PLAIN) {
+    simt_tile(dtype, &bm, &bn, &bk);
+    per_sm = 2;
+  } else {
+    tc_tile(&bm, &bn, &bk);
+    per_sm = 1;
+  }
+  const int64_t tiles = ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
+  const int64_t ksteps = (hp.K + bk - 1) / bk;
+  int64_t s = 1;
+  if (ctx->split_k > 0) {
+    s = ctx->split_k;
+  } else {
+    const int64_t target = int64_t(ctx->num_sms) * per_sm;
+    if (tiles < target / 2 && ksteps >= 8)
+      s = std::min<int64_t>((target + tiles - 1) / tiles, ksteps / 4);
+  }
+  s = std::max<int64_t>(1, std::min<int64_t>({s, ksteps, 4096}));
+  while (s > 1 && size_t(s) * size_t(hp.M) * size_t(hp.N) * elem > kMaxWorkBytes) --s;
+  const int64_t steps_per = (ksteps + s - 1) / s;
+  *k_per_split = steps_per * bk;
+  return static_cast<int>((ksteps + steps_per - 1) / steps_per);
+}
+
+int ensure_work(t1m_context* ctx, size_t bytes) {
+  if (ctx->work_bytes >= bytes) return T1M_OK;
+  if (ctx->work) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->work);
+  }
+  ctx->work = nullptr;
+  ctx->work_bytes = 0;
+  cudaError_t e = cudaMalloc(&ctx->work, bytes);
+  if (e != cudaSuccess)
+    return fail(ctx, T1M_ERR_ALLOC, std::string("split-K workspace: ") + cudaGetErrorString(e));
+  ctx->work_bytes = bytes;
+  return T1M_OK;
 }
 
 }  // namespace
@@ -236,7 +292,14 @@ int t1m_create(t1m_context** out, int device) {
     return T1M_ERR_CUDA;
   }
   ctx->stream = ctx->own_stream;
+  ctx->num_sms = prop.multiProcessorCount;
   *out = ctx;
+  return T1M_OK;
+}
+
+int t1m_set_split_k(t1m_context* ctx, int splits) {
+  if (!ctx || splits < 0 || splits > 4096) return T1M_ERR_INVALID_ARGUMENT;
+  ctx->split_k = splits;
   return T1M_OK;
 }
 
@@ -250,6 +313,7 @@ int t1m_destroy(t1m_context* ctx) {
   for (int i = 0; i < 6; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->d_err) cudaFree(ctx->d_err);
+  if (ctx->work) cudaFree(ctx->work);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return T1M_OK;
@@ -436,22 +500,51 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
 
   int kernels = 0;
   int used_method = method;
+  int splits = 1;
   if (hp.M > 0 && hp.N > 0) {
+    g.k_per_split = std::max<int64_t>(hp.K, 1);
+    g.c_split_stride = 0;
     if (hp.K == 0) {
       // C <- beta*C (or unchanged): nothing to multiply; handled by the plain
       // kernel with an empty K loop.
-      e = launch_simt(dtype, g, s, &kernels);
+      e = launch_simt(dtype, g, 1, s, &kernels);
       used_method = T1M_METHOD_PLAIN;
-    } else if (method == T1M_METHOD_PLAIN) {
-      e = launch_simt(dtype, g, s, &kernels);
     } else {
-      std::string err;
-      if (!tc_supported(method, dtype, hp))
+      if (method != T1M_METHOD_PLAIN && !tc_supported(method, dtype, hp))
         return fail(ctx, T1M_ERR_UNSUPPORTED,
                     std::string("method ") + std::to_string(method) +
                         " is not available for this dtype/contraction");
-      e = launch_tc(method, dtype, g, hp, s, ctx->d_err, &kernels, &err);
-      if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
+      int64_t kps = hp.K;
+      splits = choose_splits(ctx, method, dtype, hp, es, &kps);
+      // Split-K: the main kernel writes raw partial products (alpha = 1,
+      // beta = 0) into dense workspace slices, m fastest; the reduction sums
+      // them in FP64 and applies the epilogue.
+      GemmArgs gm = g;
+      if (splits > 1) {
+        if (int st = ensure_work(ctx, size_t(splits) * size_t(hp.M) * size_t(hp.N) * es)) return st;
+        gm.C = ctx->work;
+        gm.rsC = nullptr;
+        gm.csC = nullptr;
+        gm.uC_m = 1;
+        gm.uC_n = hp.M;
+        gm.alpha[0] = 1.0;
+        gm.alpha[1] = 0.0;
+        gm.beta[0] = gm.beta[1] = 0.0;
+        gm.flags = (g.flags & (kFlagConjA | kFlagConjB)) | kFlagBetaZero;
+        gm.k_per_split = kps;
+        gm.c_split_stride = hp.M * hp.N;
+      }
+      if (method == T1M_METHOD_PLAIN) {
+        e = launch_simt(dtype, gm, splits, s, &kernels);
+      } else {
+        std::string err;
+        e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &kernels, &err);
+        if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
+      }
+      if (e == cudaSuccess && splits > 1) {
+        e = launch_splitk_reduce(dtype, ctx->work, splits, g, s);
+        ++kernels;
+      }
     }
     if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
   }
@@ -471,7 +564,7 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
   if (report) {
     std::memset(report, 0, sizeof(*report));
     report->method = used_method;
-    report->split_k = 1;
+    report->split_k = splits;
     report->m = hp.M;
     report->n = hp.N;
     report->k = hp.K;

@@ -65,6 +65,10 @@ struct GemmArgs {
   double alpha[2];
   double beta[2];
   uint32_t flags;  // kFlag* below
+  // Split-K: CTA row blockIdx.y handles K range [y*k_per_split, ...) and, when
+  // c_split_stride != 0, writes its partial product to C + y*c_split_stride.
+  int64_t k_per_split;
+  int64_t c_split_stride;
 };
 
 constexpr uint32_t kFlagAccumulate = 1u;  // C += alpha*AB (beta ignored)
@@ -72,9 +76,17 @@ constexpr uint32_t kFlagConjA = 2u;
 constexpr uint32_t kFlagConjB = 4u;
 constexpr uint32_t kFlagBetaZero = 16u;  // BLAS semantics with beta == 0
 
-// Launchers (simt.cu).  Return cudaError_t of the launch.
-cudaError_t launch_simt(int dtype, const GemmArgs& args, cudaStream_t stream,
+// Launchers.  Return cudaError_t of the launch.
+// simt.cu: plain FP32/FP64 kernel; `splits` CTA rows along K.
+cudaError_t launch_simt(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
                         int* kernels);
+// Output tile sizes of the plain kernel for a dtype (for split decisions).
+void simt_tile(int dtype, int* bm, int* bn, int* bk);
+
+// splitk.cu: C <- alpha * sum_s W[s] + beta*C (or C + alpha*sum) with the sum
+// in FP64.  W holds `splits` dense M x N partials, m fastest, of the dtype.
+cudaError_t launch_splitk_reduce(int dtype, const void* work, int splits, const GemmArgs& out,
+                                 cudaStream_t stream);
 
 }  // namespace gb300
 }  // namespace t1m

@@ -111,8 +111,12 @@ simt_contract(const GemmArgs args) {
 
   const T* __restrict__ A = static_cast<const T*>(args.A);
   const T* __restrict__ B = static_cast<const T*>(args.B);
-  T* __restrict__ C = static_cast<T*>(args.C);
-  const int64_t M = args.M, N = args.N, K = args.K;
+  const int64_t M = args.M, N = args.N;
+  // Split-K: this CTA row covers K range [kb, K); a split writes its partial
+  // product to its own slice of the workspace.
+  const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
+  const int64_t K = min(args.K, kb + args.k_per_split);
+  T* __restrict__ C = static_cast<T*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
   const bool conjA = args.flags & kFlagConjA;
   const bool conjB = args.flags & kFlagConjB;
 
@@ -188,15 +192,15 @@ simt_contract(const GemmArgs args) {
 #pragma unroll
     for (int j = 0; j < TN; ++j) acc[i][j] = zero<T>();
 
-  const int64_t ksteps = (K + BK - 1) / BK;
+  const int64_t ksteps = (K - kb + BK - 1) / BK;
   if (ksteps > 0) {
-    load_tiles(0);
+    load_tiles(kb);
     store_tiles(0);
   }
   __syncthreads();
   for (int64_t s = 0; s < ksteps; ++s) {
     const int buf = static_cast<int>(s & 1);
-    if (s + 1 < ksteps) load_tiles((s + 1) * BK);
+    if (s + 1 < ksteps) load_tiles(kb + (s + 1) * BK);
 #pragma unroll
     for (int k = 0; k < BK; ++k) {
       T a[TM], b[TN];
@@ -246,25 +250,37 @@ simt_contract(const GemmArgs args) {
 }
 
 template <class T, int TM, int TN, int BK>
-cudaError_t launch(const GemmArgs& args, cudaStream_t stream) {
+cudaError_t launch(const GemmArgs& args, int splits, cudaStream_t stream) {
   constexpr int BM = 16 * TM, BN = 16 * TN;
   const int64_t tiles = ((args.M + BM - 1) / BM) * ((args.N + BN - 1) / BN);
   if (tiles == 0) return cudaSuccess;
   if (tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  simt_contract<T, TM, TN, BK><<<static_cast<unsigned>(tiles), kThreads, 0, stream>>>(args);
+  if (splits < 1 || splits > 65535) return cudaErrorInvalidConfiguration;
+  const dim3 grid(static_cast<unsigned>(tiles), static_cast<unsigned>(splits));
+  simt_contract<T, TM, TN, BK><<<grid, kThreads, 0, stream>>>(args);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-cudaError_t launch_simt(int dtype, const GemmArgs& args, cudaStream_t stream,
+void simt_tile(int dtype, int* bm, int* bn, int* bk) {
+  switch (dtype) {
+    case 0: *bm = 128; *bn = 128; break;
+    case 1: *bm = 128; *bn = 64; break;
+    case 2: *bm = 64; *bn = 128; break;
+    default: *bm = 64; *bn = 64; break;
+  }
+  *bk = 8;
+}
+
+cudaError_t launch_simt(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
                         int* kernels) {
   *kernels = 1;
   switch (dtype) {
-    case 0: return launch<float, 8, 8, 8>(args, stream);
-    case 1: return launch<double, 8, 4, 8>(args, stream);
-    case 2: return launch<float2, 4, 8, 8>(args, stream);
-    case 3: return launch<double2, 4, 4, 8>(args, stream);
+    case 0: return launch<float, 8, 8, 8>(args, splits, stream);
+    case 1: return launch<double, 8, 4, 8>(args, splits, stream);
+    case 2: return launch<float2, 4, 8, 8>(args, splits, stream);
+    case 3: return launch<double2, 4, 4, 8>(args, splits, stream);
   }
   return cudaErrorInvalidValue;
 }

@@ -1,0 +1,114 @@
+// Split-K reduction: C <- alpha * sum_s W[s] + beta * C (or C + alpha*sum under
+// the reference's accumulate semantics), summed in FP64.
+//
+// The reference streams K in KC-sized chunks and scatter-adds every chunk's
+// micro-tile into C (include/t1m/t1m.h:512-548).  Here, when a contraction has
+// too few output tiles to fill the GPU (skinny M*N, long K) the K range is
+// split across CTA rows; each split writes its partial product, dense and m
+// fastest, into a workspace slice, and this kernel sums the slices in double
+// precision and applies the epilogue through C's scatter vectors.  The FP64
+// sum also keeps long contractions accurate: each partial only accumulates
+// K/splits terms in FP32.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+
+#include "internal.h"
+
+namespace t1m {
+namespace gb300 {
+namespace {
+
+__device__ __forceinline__ int64_t offs(const int64_t* v, int64_t u, int64_t i) {
+  return u >= 0 ? i * u : __ldg(v + i);
+}
+
+template <class W> struct Wide;
+template <> struct Wide<float> {
+  static constexpr bool cplx = false;
+};
+template <> struct Wide<double> {
+  static constexpr bool cplx = false;
+};
+template <> struct Wide<float2> {
+  static constexpr bool cplx = true;
+};
+template <> struct Wide<double2> {
+  static constexpr bool cplx = true;
+};
+
+__device__ __forceinline__ double2 widen(float v) { return make_double2(v, 0.0); }
+__device__ __forceinline__ double2 widen(double v) { return make_double2(v, 0.0); }
+__device__ __forceinline__ double2 widen(float2 v) { return make_double2(v.x, v.y); }
+__device__ __forceinline__ double2 widen(double2 v) { return v; }
+
+__device__ __forceinline__ void narrow(double2 v, float* p) { *p = static_cast<float>(v.x); }
+__device__ __forceinline__ void narrow(double2 v, double* p) { *p = v.x; }
+__device__ __forceinline__ void narrow(double2 v, float2* p) {
+  *p = make_float2(static_cast<float>(v.x), static_cast<float>(v.y));
+}
+__device__ __forceinline__ void narrow(double2 v, double2* p) { *p = v; }
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256)
+splitk_reduce(const T* __restrict__ work, int splits, const GemmArgs out) {
+  const int64_t M = out.M, N = out.N, MN = M * N;
+  const double2 alpha = make_double2(out.alpha[0], out.alpha[1]);
+  const double2 beta = make_double2(out.beta[0], out.beta[1]);
+  const bool accumulate = out.flags & kFlagAccumulate;
+  const bool beta_zero = out.flags & kFlagBetaZero;
+  T* __restrict__ C = static_cast<T*>(out.C);
+  for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < MN;
+       idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int s = 0; s < splits; ++s) {
+      const double2 v = widen(work[s * MN + idx]);
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    const int64_t m = idx % M, n = idx / M;
+    T* p = C + offs(out.rsC, out.uC_m, m) + offs(out.csC, out.uC_n, n);
+    double2 r = cmul(alpha, acc);
+    if (accumulate) {
+      const double2 o = widen(*p);
+      r.x += o.x;
+      r.y += o.y;
+    } else if (!beta_zero) {
+      const double2 o = cmul(beta, widen(*p));
+      r.x += o.x;
+      r.y += o.y;
+    }
+    narrow(r, p);
+  }
+}
+
+template <class T>
+cudaError_t launch(const void* work, int splits, const GemmArgs& out, cudaStream_t stream) {
+  const int64_t mn = out.M * out.N;
+  if (mn == 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((mn + 255) / 256, 152 * 16);
+  splitk_reduce<T><<<static_cast<unsigned>(blocks), 256, 0, stream>>>(
+      static_cast<const T*>(work), splits, out);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_splitk_reduce(int dtype, const void* work, int splits, const GemmArgs& out,
+                                 cudaStream_t stream) {
+  switch (dtype) {
+    case 0: return launch<float>(work, splits, out, stream);
+    case 1: return launch<double>(work, splits, out, stream);
+    case 2: return launch<float2>(work, splits, out, stream);
+    case 3: return launch<double2>(work, splits, out, stream);
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace gb300
+}  // namespace t1m

@@ -228,7 +228,10 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot_ptr;
 
-  const int64_t M = args.M, N = args.N, K = args.K;
+  const int64_t M = args.M, N = args.N;
+  // Split-K: this CTA row covers K range [kb, K) (kb a multiple of kStepK).
+  const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
+  const int64_t K = min(args.K, kb + args.k_per_split);
   const int64_t tiles_m = (M + kTileMc - 1) / kTileMc;
   const int64_t tiles_n = (N + kTileN - 1) / kTileN;
   // Groups of 16 M-tiles sweep N so CTAs running together share B in L2.
@@ -240,7 +243,7 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
   const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
   const int64_t tn = (t % (G * tiles_n)) / gsize;
   const int64_t m0 = tm * kTileMc, n0 = tn * kTileN;
-  const int64_t ksteps = (K + kStepK - 1) / kStepK;
+  const int64_t ksteps = (K - kb + kStepK - 1) / kStepK;
 
   if (warp == 0) {
     // ---------------------------------------------------------- MMA issue ---
@@ -293,7 +296,7 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
     for (int64_t s = 0; s < ksteps; ++s) {
       const int r = static_cast<int>(s % kRaw);
       const uint32_t ph = static_cast<uint32_t>((s / kRaw) & 1);
-      const int64_t k0 = s * kStepK;
+      const int64_t k0 = kb + s * kStepK;
       if (kGather || lt == 0) {
         if (!ptx::mbar_wait(raw_empty(r), ph ^ 1u)) {
           record_error(err_flag, kErrRawWait);
@@ -508,7 +511,8 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
       const bool beta_zero = args.flags & kFlagBetaZero;
       const float ar = (float)args.alpha[0], ai = (float)args.alpha[1];
       const float br = (float)args.beta[0], bi = (float)args.beta[1];
-      float2* __restrict__ Cp = static_cast<float2*>(args.C);
+      float2* __restrict__ Cp =
+          static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
       const int64_t rowC = row_ok ? offs(args.rsC, args.uC_m, m0 + ci) : 0;
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
@@ -587,7 +591,7 @@ bool make_map(CUtensorMap* map, const void* base, int64_t inner, int64_t outer,
 
 template <int AMode, int BMode>
 cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
-                         int* err_flag, unsigned tiles) {
+                         int* err_flag, dim3 tiles) {
   static bool attr_set = false;
   if (!attr_set) {
     cudaError_t e = cudaFuncSetAttribute(tc3xtf32_contract<AMode, BMode>,
@@ -601,7 +605,7 @@ cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t
 
 template <int AMode>
 cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
-                     int* err_flag, unsigned tiles) {
+                     int* err_flag, dim3 tiles) {
   switch (bmode) {
     case kTmaNK: return launch_modes<AMode, kTmaNK>(args, maps, stream, err_flag, tiles);
     case kTmaKN: return launch_modes<AMode, kTmaKN>(args, maps, stream, err_flag, tiles);
@@ -611,13 +615,20 @@ cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaS
 
 }  // namespace
 
+void tc_tile(int* bm, int* bn, int* bk) {
+  *bm = kTileMc;
+  *bn = kTileN;
+  *bk = kStepK;
+}
+
 bool tc_supported(int method, int dtype, const HostPlan& plan) {
   (void)plan;
   return method == T1M_METHOD_TC_3XTF32 && dtype == T1M_COMPLEX64;
 }
 
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
-                      cudaStream_t stream, int* err_flag, int* kernels, std::string* err) {
+                      int splits, cudaStream_t stream, int* err_flag, int* kernels,
+                      std::string* err) {
   *kernels = 0;
   if (!tc_supported(method, dtype, plan)) {
     *err = "tensor-core method not available for this dtype";
@@ -644,7 +655,9 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
            make_map(&maps.b, args.B, args.N, args.K, plan.uB_k, 2 * kTileN, kStepK, false))
     bmode = kTmaKN;
   cudaError_t e;
-  const unsigned nt = static_cast<unsigned>(tiles);
+  if (splits < 1 || splits > 65535 || (splits > 1 && args.k_per_split % kStepK != 0))
+    return cudaErrorInvalidConfiguration;
+  const dim3 nt(static_cast<unsigned>(tiles), static_cast<unsigned>(splits));
   switch (amode) {
     case kTmaMK: e = launch_b<kTmaMK>(bmode, args, maps, stream, err_flag, nt); break;
     case kTmaKM: e = launch_b<kTmaKM>(bmode, args, maps, stream, err_flag, nt); break;

@@ -172,6 +172,70 @@ def test_config2_full_size_plain(ctx, torch_cuda, cfg, layout, dt):
     ctx.set_method("auto")
 
 
+@pytest.mark.slow
+@pytest.mark.parametrize("layout", ["col", "row"])
+@pytest.mark.parametrize("cfg", range(len(CFG2)))
+def test_config2_full_size_tensor_core(ctx, torch_cuda, cfg, layout):
+    """complex64 config 2 on the tensor cores (3xTF32, automatic split-K for the
+    skinny permuted case): the 1e-6 bar against sampled FP64."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    la, lb, lc, ext = CFG2[cfg]
+    da, db, dc = ([ext[ch] for ch in s] for s in (la, lb, lc))
+    strides = [(no.col_major_strides if layout == "col" else no.row_major_strides)(d)
+               for d in (da, db, dc)]
+    rng = np.random.default_rng(12)
+    dt = np.complex64
+    fa, fb = _rand(rng, int(np.prod(da)), dt), _rand(rng, int(np.prod(db)), dt)
+    fc0 = _rand(rng, int(np.prod(dc)), dt)
+    alpha, beta = 1 + 0.5j, 0.25
+    ctx.set_method("tc_3xtf32")
+    L = _layout(t1m, layout)
+    ga, gb, gc = (torch.from_numpy(x.copy()).cuda() for x in (fa, fb, fc0))
+    rep = t1m.contract_scaled(alpha, t1m.tensor(da, ga, L), la, t1m.tensor(db, gb, L), lb,
+                              beta, t1m.tensor(dc, gc, L), lc, ctx=ctx)
+    torch.cuda.synchronize()
+    mx, fro = _sampled_check(fa, fb, gc.cpu().numpy(), fc0, la, lb, lc, da, db, dc, strides,
+                             alpha, beta)
+    assert mx < 1e-6 and fro < 1e-6, (mx, fro, rep.split_k)
+    assert rep.method == 2
+    if cfg == 1:
+        assert rep.split_k > 1 and rep.kernels == 2
+    ctx.set_method("auto")
+
+
+@pytest.mark.parametrize("method", ["plain", "tc_3xtf32"])
+@pytest.mark.parametrize("splits", [2, 3, 7])
+@pytest.mark.parametrize("key", ["cfg2b_small__c64__col", "cfg3_small__c64__row",
+                                 "ragged_odd__c64__col", "ragged_odd__f64__row",
+                                 "cfg2a_small__c128__col"])
+def test_forced_split_k(ctx, key, splits, method):
+    """Split-K (partials in a workspace, FP64 reduction) gives the same result
+    as the reference on the committed fixtures, for any split count."""
+    import t1m_gb300 as t1m
+    meta, fa, fb, fc0, fc = _fixture(key)
+    if method != "plain" and fa.dtype != np.complex64:
+        pytest.skip("tensor-core method is complex64")
+    (la, lb, lc), (da, db, dc) = meta["labels"], meta["dims"]
+    L = _layout(t1m, meta["layout"])
+    ctx.set_method(method)
+    ctx.set_split_k(splits)
+    try:
+        c = fc0.copy()
+        a, b, cc = t1m.tensor(da, fa, L), t1m.tensor(db, fb, L), t1m.tensor(dc, c, L)
+        if fa.dtype.kind == "c":
+            rep = t1m.contract(a, la, b, lb, cc, lc, ctx=ctx)
+        else:
+            rep = t1m.contract(meta["alpha"], a, la, b, lb, 0.0, cc, lc, ctx=ctx)
+    finally:
+        ctx.set_split_k(0)
+        ctx.set_method("auto")
+    assert rep.split_k > 1 or rep.k <= 16
+    scale = max(np.abs(fc).max(), 1e-30)
+    err = np.abs(c.astype(np.complex128) - fc.astype(np.complex128)).max() / scale
+    assert err < TOL[fa.dtype], err
+
+
 def test_edge_cases(ctx, torch_cuda):
     """Zero extents, an outer product (empty K), a full contraction to a
     0-mode C, and non-contiguous views."""
