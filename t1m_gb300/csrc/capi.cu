@@ -31,6 +31,9 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args,
                       int* err_flag, int* kernels, std::string* err);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
 void tc_tile(int* bm, int* bn, int* bk);
+cudaError_t launch_dmma(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
+                        int* kernels);
+void dmma_tile(int* bm, int* bn, int* bk);
 }  // namespace gb300
 }  // namespace t1m
 
@@ -203,6 +206,9 @@ int choose_splits(const t1m_context* ctx, int method, int dtype, const HostPlan&
   if (method == T1M_METHOD_PLAIN) {
     simt_tile(dtype, &bm, &bn, &bk);
     per_sm = 2;
+  } else if (method == T1M_METHOD_DMMA) {
+    dmma_tile(&bm, &bn, &bk);
+    per_sm = 8;
   } else {
     tc_tile(&bm, &bn, &bk);
     per_sm = 1;
@@ -510,7 +516,9 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
       e = launch_simt(dtype, g, 1, s, &kernels);
       used_method = T1M_METHOD_PLAIN;
     } else {
-      if (method != T1M_METHOD_PLAIN && !tc_supported(method, dtype, hp))
+      const bool dmma_ok =
+          method == T1M_METHOD_DMMA && (dtype == T1M_FLOAT64 || dtype == T1M_COMPLEX128);
+      if (method != T1M_METHOD_PLAIN && !dmma_ok && !tc_supported(method, dtype, hp))
         return fail(ctx, T1M_ERR_UNSUPPORTED,
                     std::string("method ") + std::to_string(method) +
                         " is not available for this dtype/contraction");
@@ -536,6 +544,8 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
       }
       if (method == T1M_METHOD_PLAIN) {
         e = launch_simt(dtype, gm, splits, s, &kernels);
+      } else if (method == T1M_METHOD_DMMA) {
+        e = launch_dmma(dtype, gm, splits, s, &kernels);
       } else {
         std::string err;
         e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &kernels, &err);

@@ -42,6 +42,8 @@ def _methods_for(dtype):
     ms = ["plain"]
     if np.dtype(dtype) == np.complex64:
         ms.append("tc_3xtf32")
+    if np.dtype(dtype) in (np.complex128, np.float64):
+        ms.append("dmma")
     return ms
 
 
