@@ -137,6 +137,35 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha,
                  const char* labels_b, const void* beta, const t1m_tensor* c,
                  const char* labels_c, uint32_t flags, t1m_report* report);
 
+/* Contraction that allocates no memory.  No counterpart in the reference
+ * (which allocates its packing workspace with aligned_alloc on every call,
+ * t1m.h:450-460).
+ *
+ * For callers that cannot call cudaMalloc/cudaFree: applications that own all
+ * device memory through their own pool or a fixed budget, and loops where an
+ * allocation or a device-synchronising cudaFree is not acceptable.
+ * t1m_contract allocates plan buffers, staging buffers and a split-K
+ * workspace; this entry point instead uses one fixed scratch array of
+ * T1M_NOALLOC_SCRATCH_BYTES that the library holds on every GPU that loads it
+ * until the process exits (scatter vectors, split-K partial products, the
+ * kernels' error word).  Same semantics, methods, flags and status codes as
+ * t1m_contract, with these differences:
+ *   - a, b, c must be device pointers; `stream` is a cudaStream_t (NULL = the
+ *     legacy default stream); the call waits for that stream before returning;
+ *   - a contraction whose scatter vectors do not fit the scratch is rejected
+ *     (T1M_ERR_UNSUPPORTED); the split-K count shrinks to fit;
+ *   - all calls share the one scratch array and each overwrites it: calls that
+ *     overlap on the GPU (other host threads or streams) race;
+ *   - the first call on a device looks up the scratch address; make that call
+ *     before any stream capture.
+ * On failure a message is written to err (err_len bytes, may be 0). */
+#define T1M_NOALLOC_SCRATCH_BYTES (64u << 20)
+int t1m_contract_noalloc(void* stream, int method, int dtype, const void* alpha,
+                         const t1m_tensor* a, const char* labels_a, const t1m_tensor* b,
+                         const char* labels_b, const void* beta, const t1m_tensor* c,
+                         const char* labels_c, uint32_t flags, char* err,
+                         int32_t err_len);
+
 /* Result of label analysis (no GPU needed). */
 typedef struct t1m_plan_info {
   int64_t m, n, k;           /* products of the free-A, free-B, contracted extents */

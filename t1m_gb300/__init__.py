@@ -123,6 +123,8 @@ def lib() -> C.CDLL:
                                    C.c_char_p, u32, C.POINTER(Report)]
         h.t1m_analyze.argtypes = [i32, tp, C.c_char_p, tp, C.c_char_p, tp, C.c_char_p,
                                   C.POINTER(PlanInfo), C.c_char_p, C.c_int32]
+        h.t1m_contract_noalloc.argtypes = [vp, i32, i32, vp, tp, C.c_char_p, tp, C.c_char_p,
+                                           vp, tp, C.c_char_p, u32, C.c_char_p, C.c_int32]
         _lib_handle = h
     return _lib_handle
 
