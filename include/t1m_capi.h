@@ -137,6 +137,20 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha,
                  const char* labels_b, const void* beta, const t1m_tensor* c,
                  const char* labels_c, uint32_t flags, t1m_report* report);
 
+/* Adjoint (vector-Jacobian product) of C = A*B for a real loss L, in the
+ * conjugate-Wirtinger convention PyTorch uses for complex autograd:
+ *   dA = dC * conj(B)   (labels: dC[labels_c], B[labels_b] -> dA[labels_a])
+ *   dB = conj(A) * dC   (labels: A[labels_a], dC[labels_c] -> dB[labels_b])
+ * da or db may be NULL (not computed).  Without T1M_FLAG_ACCUMULATE the
+ * gradients are overwritten, with it they are added.  Both products run on
+ * the same kernels as t1m_contract with conjugate-on-load, so the method and
+ * split-K settings of the context apply.  No counterpart in the reference
+ * (which has no differentiation); the report (if any) sums both products. */
+int t1m_contract_vjp(t1m_context* ctx, int dtype, const t1m_tensor* dc,
+                     const char* labels_c, const t1m_tensor* a, const char* labels_a,
+                     const t1m_tensor* b, const char* labels_b, const t1m_tensor* da,
+                     const t1m_tensor* db, uint32_t flags, t1m_report* report);
+
 /* Contraction that allocates no memory.  No counterpart in the reference
  * (which allocates its packing workspace with aligned_alloc on every call,
  * t1m.h:450-460).

@@ -125,6 +125,8 @@ def lib() -> C.CDLL:
                                   C.POINTER(PlanInfo), C.c_char_p, C.c_int32]
         h.t1m_contract_noalloc.argtypes = [vp, i32, i32, vp, tp, C.c_char_p, tp, C.c_char_p,
                                            vp, tp, C.c_char_p, u32, C.c_char_p, C.c_int32]
+        h.t1m_contract_vjp.argtypes = [vp, i32, tp, C.c_char_p, tp, C.c_char_p, tp, C.c_char_p,
+                                       tp, tp, u32, C.POINTER(Report)]
         _lib_handle = h
     return _lib_handle
 
@@ -292,6 +294,29 @@ def contract_scaled(alpha, a: tensor, la: str, b: tensor, lb: str, beta, c: tens
     counterpart; the reference has no complex scalars, t1m.h:570-577)."""
     flags = (FLAG_CONJ_A if conj_a else 0) | (FLAG_CONJ_B if conj_b else 0)
     return contract_raw(alpha, a, la, b, lb, beta, c, lc, flags, ctx)
+
+
+def contract_vjp(dc: tensor, lc: str, a: tensor, la: str, b: tensor, lb: str,
+                 da: tensor | None = None, db: tensor | None = None,
+                 accumulate: bool = False, ctx: Context | None = None) -> Report:
+    """Adjoint of C = A*B: dA = dC*conj(B), dB = conj(A)*dC (conjugate-Wirtinger
+    convention of PyTorch's complex autograd).  da/db may be None."""
+    ctx = ctx or default_context()
+    dts = {dc.dtype(), a.dtype(), b.dtype()}
+    if len(dts) != 1:
+        raise TypeError(f"mixed element types {dts}")
+    dtype = _DTYPE_OF[dts.pop()]
+    keep: list = []
+    tdc, ta, tb = dc._c(keep), a._c(keep), b._c(keep)
+    pda = C.byref(da._c(keep)) if da is not None else None
+    pdb = C.byref(db._c(keep)) if db is not None else None
+    rep = Report()
+    st = lib().t1m_contract_vjp(ctx.handle, dtype, C.byref(tdc), lc.encode(), C.byref(ta),
+                                la.encode(), C.byref(tb), lb.encode(), pda, pdb,
+                                FLAG_ACCUMULATE if accumulate else 0, C.byref(rep))
+    if st != OK:
+        raise T1MError(st, (lib().t1m_last_error(ctx.handle) or b"").decode())
+    return rep
 
 
 def analyze(a: tensor, la: str, b: tensor, lb: str, c: tensor, lc: str) -> dict:

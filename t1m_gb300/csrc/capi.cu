@@ -596,3 +596,45 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
 }
 
 }  // extern "C"
+
+extern "C" int t1m_contract_vjp(t1m_context* ctx, int dtype, const t1m_tensor* dc,
+                                const char* lc, const t1m_tensor* a, const char* la,
+                                const t1m_tensor* b, const char* lb, const t1m_tensor* da,
+                                const t1m_tensor* db, uint32_t flags, t1m_report* report) {
+  if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
+  if (!dc || !a || !b || !lc || !la || !lb) return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "null argument");
+  if (elem_size(dtype) == 0) return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "unknown dtype");
+  // One and zero of the dtype (complex: re, im).
+  const double one_d[2] = {1.0, 0.0}, zero_d[2] = {0.0, 0.0};
+  const float one_f[2] = {1.0f, 0.0f}, zero_f[2] = {0.0f, 0.0f};
+  const bool single = dtype == T1M_FLOAT32 || dtype == T1M_COMPLEX64;
+  const void* one = single ? static_cast<const void*>(one_f) : static_cast<const void*>(one_d);
+  const void* zero = single ? static_cast<const void*>(zero_f) : static_cast<const void*>(zero_d);
+  const uint32_t base = flags & (T1M_FLAG_ACCUMULATE | T1M_FLAG_NO_TIMING);
+  t1m_report r1{}, r2{};
+  if (da) {
+    // dA[la] = sum over the free-B labels of dC[lc] * conj(B[lb]).
+    const int st = t1m_contract(ctx, dtype, one, dc, lc, b, lb, zero, da, la,
+                                base | T1M_FLAG_CONJ_B, report ? &r1 : nullptr);
+    if (st != T1M_OK) return st;
+  }
+  if (db) {
+    // dB[lb] = sum over the free-A labels of conj(A[la]) * dC[lc].
+    const int st = t1m_contract(ctx, dtype, one, a, la, dc, lc, zero, db, lb,
+                                base | T1M_FLAG_CONJ_A, report ? &r2 : nullptr);
+    if (st != T1M_OK) return st;
+  }
+  if (report) {
+    *report = da ? r1 : r2;
+    if (da && db) {
+      report->flops = r1.flops + r2.flops;
+      report->kernel_ms = r1.kernel_ms + r2.kernel_ms;
+      report->h2d_ms = r1.h2d_ms + r2.h2d_ms;
+      report->d2h_ms = r1.d2h_ms + r2.d2h_ms;
+      report->h2d_bytes = r1.h2d_bytes + r2.h2d_bytes;
+      report->d2h_bytes = r1.d2h_bytes + r2.d2h_bytes;
+      report->kernels = r1.kernels + r2.kernels;
+    }
+  }
+  return T1M_OK;
+}
