@@ -151,6 +151,42 @@ int t1m_contract_vjp(t1m_context* ctx, int dtype, const t1m_tensor* dc,
                      const t1m_tensor* b, const char* labels_b, const t1m_tensor* da,
                      const t1m_tensor* db, uint32_t flags, t1m_report* report);
 
+/* Grouped batches: many contractions of uneven shapes (for example the
+ * updates of a tensor-network sweep) run as grouped launches instead of one
+ * launch per call.  The reference has no batching (its counterpart is a loop
+ * of t1m::contract calls, t1m.h:560-577).  All tensors are device pointers.
+ * An item may read the C of an EARLIER item (depends_on = its index); every
+ * complex64 item with at least 32 rows and columns runs on the persistent
+ * tensor-core kernel, the rest on the grouped plain kernel (a skinny tile for
+ * outputs with at most 16 columns).  With T1M_GROUP_AUTOTUNE the family of
+ * each shape class (log2 buckets of M, N, K) is measured once and cached in a
+ * versioned file ($T1M_TUNE_CACHE, default $HOME/.cache/t1m_gb300_tune.txt,
+ * keyed by GPU name, SM count and driver).  With T1M_GROUP_GRAPH the launches
+ * are captured once into a CUDA graph that t1m_group_launch replays. */
+typedef struct t1m_group_item {
+  const t1m_tensor* a;
+  const char* labels_a;
+  const t1m_tensor* b;
+  const char* labels_b;
+  const t1m_tensor* c;
+  const char* labels_c;
+  double alpha[2];     /* re, im (im ignored for real dtypes) */
+  double beta[2];
+  int32_t depends_on;  /* index of an earlier item whose C this item reads, or -1 */
+  uint32_t flags;      /* T1M_FLAG_ACCUMULATE / _CONJ_A / _CONJ_B */
+} t1m_group_item;
+
+typedef struct t1m_group t1m_group;
+
+#define T1M_GROUP_GRAPH 1u
+#define T1M_GROUP_AUTOTUNE 2u
+
+int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_group_item* items,
+                     uint32_t options, t1m_group** group);
+/* Run the batch on the context's stream; with a report, wait and time it. */
+int t1m_group_launch(t1m_group* group, t1m_report* report);
+int t1m_group_destroy(t1m_group* group);
+
 /* Contraction that allocates no memory.  No counterpart in the reference
  * (which allocates its packing workspace with aligned_alloc on every call,
  * t1m.h:450-460).

@@ -94,6 +94,17 @@ class PlanInfo(C.Structure):
                 ("modes_n", C.c_int32), ("modes_k", C.c_int32), ("reserved", C.c_int32)]
 
 
+class GroupItem(C.Structure):
+    _fields_ = [("a", C.POINTER(_Tensor)), ("labels_a", C.c_char_p),
+                ("b", C.POINTER(_Tensor)), ("labels_b", C.c_char_p),
+                ("c", C.POINTER(_Tensor)), ("labels_c", C.c_char_p),
+                ("alpha", C.c_double * 2), ("beta", C.c_double * 2),
+                ("depends_on", C.c_int32), ("flags", C.c_uint32)]
+
+
+GROUP_GRAPH = 1
+GROUP_AUTOTUNE = 2
+
 _lib_handle: C.CDLL | None = None
 
 
@@ -127,6 +138,9 @@ def lib() -> C.CDLL:
                                            vp, tp, C.c_char_p, u32, C.c_char_p, C.c_int32]
         h.t1m_contract_vjp.argtypes = [vp, i32, tp, C.c_char_p, tp, C.c_char_p, tp, C.c_char_p,
                                        tp, tp, u32, C.POINTER(Report)]
+        h.t1m_group_create.argtypes = [vp, i32, i32, C.POINTER(GroupItem), u32, C.POINTER(vp)]
+        h.t1m_group_launch.argtypes = [vp, C.POINTER(Report)]
+        h.t1m_group_destroy.argtypes = [vp]
         _lib_handle = h
     return _lib_handle
 
@@ -317,6 +331,57 @@ def contract_vjp(dc: tensor, lc: str, a: tensor, la: str, b: tensor, lb: str,
     if st != OK:
         raise T1MError(st, (lib().t1m_last_error(ctx.handle) or b"").decode())
     return rep
+
+
+class Group:
+    """A batch of contractions run as grouped launches (t1m_group_*).
+
+    ``items``: sequence of (alpha, a, la, b, lb, beta, c, lc, depends_on)
+    with device tensors (C = alpha*A*B + beta*C; depends_on = index of an
+    earlier item whose C this one reads, or -1)."""
+
+    def __init__(self, items, ctx: Context | None = None, graph: bool = True,
+                 autotune: bool = False):
+        self.ctx = ctx or default_context()
+        self._h = C.c_void_p()
+        self._keep: list = []
+        arr = (GroupItem * max(1, len(items)))()
+        dtypes = set()
+        for i, (alpha, a, la, b, lb, beta, c, lc, dep) in enumerate(items):
+            dtypes |= {a.dtype(), b.dtype(), c.dtype()}
+            ta, tb, tc = a._c(self._keep), b._c(self._keep), c._c(self._keep)
+            self._keep += [ta, tb, tc]
+            al, be = complex(alpha), complex(beta)
+            arr[i] = GroupItem(C.pointer(ta), la.encode(), C.pointer(tb), lb.encode(),
+                               C.pointer(tc), lc.encode(), (C.c_double * 2)(al.real, al.imag),
+                               (C.c_double * 2)(be.real, be.imag), int(dep), 0)
+        if len(dtypes) > 1:
+            raise TypeError(f"mixed element types {dtypes}")
+        dtype = _DTYPE_OF[dtypes.pop()] if dtypes else COMPLEX64
+        self._keep.append(arr)
+        opts = (GROUP_GRAPH if graph else 0) | (GROUP_AUTOTUNE if autotune else 0)
+        st = lib().t1m_group_create(self.ctx.handle, dtype, len(items), arr, opts,
+                                    C.byref(self._h))
+        if st != OK:
+            raise T1MError(st, (lib().t1m_last_error(self.ctx.handle) or b"").decode())
+
+    def launch(self, timed: bool = True) -> Report | None:
+        rep = Report()
+        st = lib().t1m_group_launch(self._h, C.byref(rep) if timed else None)
+        if st != OK:
+            raise T1MError(st, (lib().t1m_last_error(self.ctx.handle) or b"").decode())
+        return rep if timed else None
+
+    def close(self) -> None:
+        if self._h:
+            lib().t1m_group_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def analyze(a: tensor, la: str, b: tensor, lb: str, c: tensor, lc: str) -> dict:

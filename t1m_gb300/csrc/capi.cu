@@ -11,6 +11,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <list>
 #include <memory>
@@ -66,7 +67,7 @@ struct t1m_context {
 
 namespace {
 
-constexpr size_t kMaxPlans = 64;
+constexpr size_t kMaxPlans = 4096;
 
 size_t elem_size(int dtype) {
   switch (dtype) {
@@ -635,6 +636,463 @@ extern "C" int t1m_contract_vjp(t1m_context* ctx, int dtype, const t1m_tensor* d
       report->d2h_bytes = r1.d2h_bytes + r2.d2h_bytes;
       report->kernels = r1.kernels + r2.kernels;
     }
+  }
+  return T1M_OK;
+}
+
+// ------------------------------------------------------------ grouped ---
+// A batch of contractions (e.g. the updates of a tensor-network sweep) run
+// as grouped launches: every complex64 contraction with enough rows and
+// columns is a list of tiles of ONE persistent tensor-core launch; the rest
+// (other dtypes, skinny outputs) are tiles of one grouped plain launch per
+// tile shape.  Items may read the C of an earlier item (depends_on); when all
+// items are tensor-core items the dependencies are resolved inside the one
+// persistent launch, otherwise items run in dependency levels.  Optionally
+// the whole batch is captured once in a CUDA graph.  The reference has no
+// batching; its counterpart is a loop of t1m::contract calls.
+#include "tc.h"
+
+namespace {
+
+enum Family : int { kFamTC = 0, kFamSimt = 1, kFamSimtSkinny = 2 };
+
+// Autotuner cache: shape class -> family, measured once per process and
+// persisted to a small versioned text file (T1M_TUNE_CACHE, default
+// $HOME/.cache/t1m_gb300_tune.txt) keyed by GPU name, SM count and driver.
+struct TuneCache {
+  std::mutex mu;
+  bool loaded = false;
+  std::string path, header;
+  std::unordered_map<std::string, int> choice;
+
+  void load(int device) {
+    const char* env_now = std::getenv("T1M_TUNE_CACHE");
+    const char* home_now = std::getenv("HOME");
+    const std::string want =
+        env_now ? env_now : (home_now ? std::string(home_now) + "/.cache/t1m_gb300_tune.txt" : "");
+    if (loaded && want == path) return;  // same file: the in-memory table is current
+    loaded = true;
+    choice.clear();
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, device);
+    int drv = 0;
+    cudaDriverGetVersion(&drv);
+    header = std::string("t1m_gb300-tune v1 ") + prop.name + " sms=" +
+             std::to_string(prop.multiProcessorCount) + " driver=" + std::to_string(drv);
+    for (char& ch : header)
+      if (ch == '\n') ch = ' ';
+    const char* env = std::getenv("T1M_TUNE_CACHE");
+    const char* home = std::getenv("HOME");
+    path = env ? env : (home ? std::string(home) + "/.cache/t1m_gb300_tune.txt" : "");
+    if (path.empty()) return;
+    FILE* f = std::fopen(path.c_str(), "r");
+    if (!f) return;
+    char line[512];
+    bool ok = std::fgets(line, sizeof(line), f) && header == std::string(line).substr(0, header.size());
+    while (ok && std::fgets(line, sizeof(line), f)) {
+      char key[400];
+      int fam = 0;
+      if (std::sscanf(line, "%399s %d", key, &fam) == 2) choice[key] = fam;
+    }
+    std::fclose(f);
+  }
+  void save() {
+    if (path.empty()) return;
+    FILE* f = std::fopen(path.c_str(), "w");
+    if (!f) return;
+    std::fprintf(f, "%s\n", header.c_str());
+    for (auto& kv : choice) std::fprintf(f, "%s %d\n", kv.first.c_str(), kv.second);
+    std::fclose(f);
+  }
+};
+TuneCache g_tune;
+
+int log2_bucket(int64_t v) {
+  int b = 0;
+  while ((int64_t(1) << (b + 1)) <= v) ++b;
+  return b;
+}
+
+std::string shape_class(int dtype, const HostPlan& hp) {
+  return std::to_string(dtype) + ":" + std::to_string(log2_bucket(hp.M)) + "," +
+         std::to_string(log2_bucket(hp.N)) + "," + std::to_string(log2_bucket(hp.K));
+}
+
+// Default family before (or without) tuning.
+int heuristic_family(int dtype, const HostPlan& hp) {
+  if (dtype == T1M_COMPLEX64 && hp.M >= 32 && hp.N >= 32) return kFamTC;
+  return hp.N <= 16 ? kFamSimtSkinny : kFamSimt;
+}
+
+}  // namespace
+
+struct t1m_group {
+  t1m_context* ctx = nullptr;
+  int dtype = 0;
+  int n = 0;
+  double flops = 0;
+  void* vectors = nullptr;      // all scatter vectors of all items
+  void* tc_dev = nullptr;       // TcProblem array
+  int* done = nullptr;          // tile-completion counters (single TC launch)
+  void* simt_dev = nullptr;     // SimtProblem arrays, per (level, family)
+  struct Launch {
+    int family;
+    int64_t offset;   // first descriptor in tc_dev / simt_dev
+    int count;
+    int64_t tiles;
+  };
+  std::vector<std::vector<Launch>> levels;
+  bool single_tc = false;
+  int64_t tc_total = 0;
+  int tc_count = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int kernels = 0;
+};
+
+namespace {
+
+int enqueue_group(t1m_group* g, cudaStream_t s) {
+  t1m_context* ctx = g->ctx;
+  cudaError_t e = cudaSuccess;
+  int kernels = 0;
+  if (g->single_tc) {
+    e = cudaMemsetAsync(g->done, 0, sizeof(int) * size_t(std::max(1, g->tc_count)), s);
+    if (e == cudaSuccess)
+      e = tc_launch_persistent(nullptr, static_cast<const TcProblem*>(g->tc_dev), g->tc_count,
+                               g->tc_total, ctx->num_sms, g->done, s, ctx->d_err);
+    kernels = 1;
+  } else {
+    for (auto& lev : g->levels) {
+      for (auto& l : lev) {
+        if (l.tiles == 0) continue;
+        if (l.family == kFamTC)
+          e = tc_launch_persistent(nullptr, static_cast<const TcProblem*>(g->tc_dev) + l.offset,
+                                   l.count, l.tiles, ctx->num_sms, nullptr, s, ctx->d_err);
+        else
+          e = launch_simt_group(g->dtype, l.family == kFamSimtSkinny,
+                                static_cast<const SimtProblem*>(g->simt_dev) + l.offset, l.count,
+                                l.tiles, s);
+        ++kernels;
+        if (e != cudaSuccess) break;
+      }
+      if (e != cudaSuccess) break;
+    }
+  }
+  g->kernels = kernels;
+  return e == cudaSuccess ? T1M_OK : cuda_fail(ctx, e, "grouped launch");
+}
+
+}  // namespace
+
+extern "C" int t1m_group_destroy(t1m_group* g) {
+  if (!g) return T1M_ERR_INVALID_ARGUMENT;
+  if (g->ctx) {
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+  }
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  if (g->vectors) cudaFree(g->vectors);
+  if (g->tc_dev) cudaFree(g->tc_dev);
+  if (g->simt_dev) cudaFree(g->simt_dev);
+  if (g->done) cudaFree(g->done);
+  delete g;
+  return T1M_OK;
+}
+
+extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_group_item* items,
+                                uint32_t options, t1m_group** out) {
+  if (!ctx || !out || n < 0 || (n > 0 && !items)) return T1M_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  const size_t es = elem_size(dtype);
+  if (es == 0) return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "unknown dtype");
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "set device");
+  std::unique_ptr<t1m_group, int (*)(t1m_group*)> g(new t1m_group(), t1m_group_destroy);
+  g->ctx = ctx;
+  g->dtype = dtype;
+  g->n = n;
+
+  // Plans, dependency levels and families.
+  std::vector<HostPlan> plans(n);
+  std::vector<int> level(n, 0), family(n, kFamSimt);
+  size_t vec_elems = 0;
+  for (int i = 0; i < n; ++i) {
+    const t1m_group_item& it = items[i];
+    if (!it.a || !it.b || !it.c || !it.labels_a || !it.labels_b || !it.labels_c)
+      return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "null member in group item " + std::to_string(i));
+    if (it.depends_on >= i)
+      return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "item " + std::to_string(i) +
+                                                      " depends on a later item");
+    int64_t sa[64], sb[64], sc[64];
+    for (const t1m_tensor* t : {it.a, it.b, it.c})
+      if (t->ndim < 0 || t->ndim > 64 || (t->ndim > 0 && !t->extents))
+        return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "bad rank in group item " + std::to_string(i));
+    if (!resolve_strides(it.a, sa) || !resolve_strides(it.b, sb) || !resolve_strides(it.c, sc))
+      return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "strided tensor without strides");
+    std::string err;
+    int st = build_plan(dtype, it.a->ndim, it.a->extents, sa, it.labels_a, it.b->ndim,
+                        it.b->extents, sb, it.labels_b, it.c->ndim, it.c->extents, sc,
+                        it.labels_c, &plans[i], &err);
+    if (st != T1M_OK) return fail(ctx, st, "group item " + std::to_string(i) + ": " + err);
+    const HostPlan& hp = plans[i];
+    if (hp.M > 0 && hp.N > 0 && hp.K > 0 &&
+        (!is_device_pointer(it.a->data) || !is_device_pointer(it.b->data) ||
+         !is_device_pointer(it.c->data)))
+      return fail(ctx, T1M_ERR_INVALID_ARGUMENT,
+                  "grouped contractions take device pointers (item " + std::to_string(i) + ")");
+    level[i] = it.depends_on >= 0 ? level[it.depends_on] + 1 : 0;
+    family[i] = heuristic_family(dtype, hp);
+    if (ctx->method == T1M_METHOD_PLAIN && family[i] == kFamTC) family[i] = kFamSimt;
+    vec_elems += hp.rsA.size() + hp.csA.size() + hp.rsB.size() + hp.csB.size() + hp.rsC.size() +
+                 hp.csC.size() + 6;
+    g->flops += (dtype >= T1M_COMPLEX64 ? 8.0 : 2.0) * double(hp.M) * double(hp.N) * double(hp.K);
+  }
+
+  // Scatter vectors of every item, one allocation.
+  e = cudaMalloc(&g->vectors, std::max<size_t>(vec_elems, 1) * sizeof(int64_t));
+  if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group scatter vectors");
+  std::vector<int64_t> host(vec_elems);
+  std::vector<GemmArgs> args(n);
+  size_t off = 0;
+  for (int i = 0; i < n; ++i) {
+    const HostPlan& hp = plans[i];
+    const t1m_group_item& it = items[i];
+    const std::vector<int64_t>* vs[6] = {&hp.rsA, &hp.csA, &hp.rsB, &hp.csB, &hp.rsC, &hp.csC};
+    const int64_t* dptr[6];
+    for (int v = 0; v < 6; ++v) {
+      std::copy(vs[v]->begin(), vs[v]->end(), host.begin() + off);
+      host[off + vs[v]->size()] = 0;
+      dptr[v] = static_cast<const int64_t*>(g->vectors) + off;
+      off += vs[v]->size() + 1;
+    }
+    GemmArgs& a = args[i];
+    a = GemmArgs{};
+    a.A = it.a->data;
+    a.B = it.b->data;
+    a.C = it.c->data;
+    a.M = hp.M;
+    a.N = hp.N;
+    a.K = hp.K;
+    a.rsA = dptr[0]; a.csA = dptr[1]; a.rsB = dptr[2]; a.csB = dptr[3];
+    a.rsC = dptr[4]; a.csC = dptr[5];
+    a.uA_m = hp.uA_m; a.uA_k = hp.uA_k; a.uB_k = hp.uB_k; a.uB_n = hp.uB_n;
+    a.uC_m = hp.uC_m; a.uC_n = hp.uC_n;
+    a.alpha[0] = it.alpha[0];
+    a.alpha[1] = it.alpha[1];
+    a.beta[0] = it.beta[0];
+    a.beta[1] = it.beta[1];
+    a.flags = 0;
+    if (it.flags & T1M_FLAG_ACCUMULATE) a.flags |= kFlagAccumulate;
+    if (it.flags & T1M_FLAG_CONJ_A) a.flags |= kFlagConjA;
+    if (it.flags & T1M_FLAG_CONJ_B) a.flags |= kFlagConjB;
+    if (!(it.flags & T1M_FLAG_ACCUMULATE) && a.beta[0] == 0.0 && a.beta[1] == 0.0)
+      a.flags |= kFlagBetaZero;
+    a.k_per_split = std::max<int64_t>(hp.K, 1);
+    a.c_split_stride = 0;
+  }
+  if (vec_elems) {
+    e = cudaMemcpy(g->vectors, host.data(), vec_elems * sizeof(int64_t), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "group scatter vectors upload");
+  }
+
+  // Autotuning: per shape class, time the candidate families once on a
+  // representative item (into a scratch output) and keep the fastest.
+  if (options & T1M_GROUP_AUTOTUNE) {
+    std::lock_guard<std::mutex> lock(g_tune.mu);
+    g_tune.load(ctx->device);
+    bool changed = false;
+    for (int i = 0; i < n; ++i) {
+      const HostPlan& hp = plans[i];
+      if (hp.M == 0 || hp.N == 0 || hp.K == 0) continue;
+      const std::string key = shape_class(dtype, hp);
+      auto it = g_tune.choice.find(key);
+      if (it != g_tune.choice.end()) {
+        family[i] = it->second;
+        continue;
+      }
+      std::vector<int> cands = {kFamSimt, kFamSimtSkinny};
+      if (dtype == T1M_COMPLEX64 && ctx->method != T1M_METHOD_PLAIN) cands.push_back(kFamTC);
+      void* scratch = nullptr;
+      if (cudaMalloc(&scratch, size_t(hp.M) * size_t(hp.N) * es) != cudaSuccess)
+        return fail(ctx, T1M_ERR_ALLOC, "autotune scratch");
+      GemmArgs probe = args[i];
+      probe.C = scratch;
+      probe.rsC = probe.csC = nullptr;
+      probe.uC_m = 1;
+      probe.uC_n = hp.M;
+      probe.flags = (probe.flags & (kFlagConjA | kFlagConjB)) | kFlagBetaZero;
+      void* pd = nullptr;
+      if (cudaMalloc(&pd, sizeof(TcProblem) > sizeof(SimtProblem) ? sizeof(TcProblem) : sizeof(SimtProblem)) != cudaSuccess) {
+        cudaFree(scratch);
+        return fail(ctx, T1M_ERR_ALLOC, "autotune descriptor");
+      }
+      float best = 1e30f;
+      int best_f = family[i];
+      for (int f : cands) {
+        float total = 0;
+        bool ok = true;
+        for (int rep = 0; rep < 3 && ok; ++rep) {
+          cudaEventRecord(ctx->ev[4], ctx->stream);
+          cudaError_t le;
+          if (f == kFamTC) {
+            TcProblem tp;
+            ok = tc_prepare(probe, hp, 1, &tp);
+            tp.tile_begin = 0;
+            tp.dep = -1;
+            le = ok ? tc_launch_persistent(&tp, nullptr, 1, tc_problem_tiles(tp), ctx->num_sms,
+                                           nullptr, ctx->stream, ctx->d_err)
+                    : cudaErrorInvalidValue;
+          } else {
+            SimtProblem sp{probe, 0};
+            cudaMemcpy(pd, &sp, sizeof(sp), cudaMemcpyHostToDevice);
+            int bm, bn;
+            simt_group_tile(dtype, f == kFamSimtSkinny, &bm, &bn);
+            const int64_t tiles = ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
+            le = launch_simt_group(dtype, f == kFamSimtSkinny, static_cast<SimtProblem*>(pd), 1,
+                                   tiles, ctx->stream);
+          }
+          cudaEventRecord(ctx->ev[5], ctx->stream);
+          if (le != cudaSuccess || cudaEventSynchronize(ctx->ev[5]) != cudaSuccess) {
+            cudaGetLastError();
+            ok = false;
+            break;
+          }
+          float ms = 0;
+          cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+          if (rep > 0) total += ms;  // first run warms up
+        }
+        if (ok && total < best) {
+          best = total;
+          best_f = f;
+        }
+      }
+      cudaFree(pd);
+      cudaFree(scratch);
+      if (int st = check_device_error(ctx)) return st;
+      family[i] = best_f;
+      g_tune.choice[key] = best_f;
+      changed = true;
+    }
+    if (changed) g_tune.save();
+  }
+
+  // Launch lists.  One persistent tensor-core launch for everything if every
+  // item is a tensor-core item (dependencies resolved in the kernel),
+  // otherwise one launch per (level, family).
+  bool all_tc = n > 0;
+  for (int i = 0; i < n; ++i) all_tc = all_tc && family[i] == kFamTC;
+  int max_level = 0;
+  for (int i = 0; i < n; ++i) max_level = std::max(max_level, level[i]);
+  std::vector<TcProblem> tcs;
+  std::vector<SimtProblem> simts;
+  std::vector<int> tc_index(n, -1);
+  g->levels.assign(max_level + 1, {});
+  for (int lv = 0; lv <= max_level; ++lv) {
+    for (int fam : {kFamTC, kFamSimt, kFamSimtSkinny}) {
+      t1m_group::Launch L{fam, fam == kFamTC ? int64_t(tcs.size()) : int64_t(simts.size()), 0, 0};
+      for (int i = 0; i < n; ++i) {
+        if (level[i] != lv || family[i] != fam) continue;
+        const HostPlan& hp = plans[i];
+        if (fam == kFamTC) {
+          TcProblem tp;
+          if (!tc_prepare(args[i], hp, 1, &tp))
+            return fail(ctx, T1M_ERR_UNSUPPORTED, "group item " + std::to_string(i) +
+                                                      " cannot run on the tensor cores");
+          tp.tile_begin = (all_tc ? g->tc_total : L.tiles);
+          tp.dep = -1;
+          tp.dep_tiles = 0;
+          if (all_tc && items[i].depends_on >= 0) {
+            const TcProblem& d = tcs[tc_index[items[i].depends_on]];
+            tp.dep = tc_index[items[i].depends_on];
+            tp.dep_tiles = static_cast<int32_t>(tc_problem_tiles(d));
+          }
+          tc_index[i] = static_cast<int>(tcs.size());
+          const int64_t t = tc_problem_tiles(tp);
+          L.tiles += t;
+          g->tc_total += t;
+          tcs.push_back(tp);
+        } else {
+          int bm, bn;
+          simt_group_tile(dtype, fam == kFamSimtSkinny, &bm, &bn);
+          SimtProblem sp{args[i], L.tiles};
+          L.tiles += ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
+          simts.push_back(sp);
+        }
+        ++L.count;
+      }
+      if (L.count > 0) g->levels[lv].push_back(L);
+    }
+  }
+  g->single_tc = all_tc && max_level > 0;
+  g->tc_count = static_cast<int>(tcs.size());
+  if (all_tc && max_level == 0) g->single_tc = false;  // one level: plain persistent launch
+  if (!tcs.empty()) {
+    e = cudaMalloc(&g->tc_dev, tcs.size() * sizeof(TcProblem));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(g->tc_dev, tcs.data(), tcs.size() * sizeof(TcProblem), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc(&g->done, sizeof(int) * tcs.size());
+    if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group descriptors");
+  }
+  if (!simts.empty()) {
+    e = cudaMalloc(&g->simt_dev, simts.size() * sizeof(SimtProblem));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(g->simt_dev, simts.data(), simts.size() * sizeof(SimtProblem),
+                     cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group descriptors");
+  }
+
+  if (options & T1M_GROUP_GRAPH) {
+    cudaStream_t cs = nullptr;
+    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "capture stream");
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int st = T1M_OK;
+    if (e == cudaSuccess) st = enqueue_group(g.get(), cs);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess || e2 != cudaSuccess || st != T1M_OK || !graph) {
+      if (graph) cudaGraphDestroy(graph);
+      return st != T1M_OK ? st : cuda_fail(ctx, e != cudaSuccess ? e : e2, "graph capture");
+    }
+    g->graph = graph;
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph instantiate");
+  }
+  *out = g.release();
+  return T1M_OK;
+}
+
+extern "C" int t1m_group_launch(t1m_group* g, t1m_report* report) {
+  if (!g || !g->ctx) return T1M_ERR_INVALID_ARGUMENT;
+  t1m_context* ctx = g->ctx;
+  cudaSetDevice(ctx->device);
+  cudaStream_t s = ctx->stream;
+  if (report) cudaEventRecord(ctx->ev[0], s);
+  int st = T1M_OK;
+  if (g->exec) {
+    const cudaError_t e = cudaGraphLaunch(g->exec, s);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph launch");
+    if (g->kernels == 0) g->kernels = 1;
+  } else {
+    st = enqueue_group(g, s);
+    if (st != T1M_OK) return st;
+  }
+  if (report) {
+    cudaEventRecord(ctx->ev[1], s);
+    cudaError_t e = cudaEventSynchronize(ctx->ev[1]);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "grouped launch");
+    if (int s2 = check_device_error(ctx)) return s2;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    std::memset(report, 0, sizeof(*report));
+    report->method = T1M_METHOD_AUTO;
+    report->split_k = 1;
+    report->flops = g->flops;
+    report->kernel_ms = ms;
+    report->kernels = g->kernels;
   }
   return T1M_OK;
 }

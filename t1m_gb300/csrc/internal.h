@@ -83,6 +83,18 @@ cudaError_t launch_simt(int dtype, const GemmArgs& args, int splits, cudaStream_
 // Output tile sizes of the plain kernel for a dtype (for split decisions).
 void simt_tile(int dtype, int* bm, int* bn, int* bk);
 
+// One contraction of a grouped plain launch (device array, sorted by
+// tile_begin; no split-K).
+struct SimtProblem {
+  GemmArgs g;
+  int64_t tile_begin;
+};
+// Tile of a grouped plain launch: the regular tile, or a skinny one (128 x 16)
+// for contractions with few output columns.
+void simt_group_tile(int dtype, bool skinny, int* bm, int* bn);
+cudaError_t launch_simt_group(int dtype, bool skinny, const SimtProblem* dev, int nprob,
+                              int64_t total_tiles, cudaStream_t stream);
+
 // splitk.cu: C <- alpha * sum_s W[s] + beta*C (or C + alpha*sum) with the sum
 // in FP64.  W holds `splits` dense M x N partials, m fastest, of the dtype.
 cudaError_t launch_splitk_reduce(int dtype, const void* work, int splits, const GemmArgs& out,

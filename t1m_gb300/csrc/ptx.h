@@ -33,6 +33,13 @@ __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
                : "memory");
 }
 
+// Arrive `count` times at once (stands in for threads that skip a phase).
+__device__ __forceinline__ void mbar_arrive_count(uint32_t bar, uint32_t count) {
+  asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.shared::cta.b64 st, [%0], %1;\n}" ::"r"(bar),
+               "r"(count)
+               : "memory");
+}
+
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("{\n .reg .b64 st;\n mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}" ::"r"(bar),
                "r"(bytes)

@@ -91,11 +91,28 @@ constexpr int kThreads = 256;
 // 16 x 16 threads; thread (tx, ty) owns rows ty*TM .. ty*TM+TM-1 of the tile
 // and columns tx + 16*j (j < TN), so shared-memory reads of B are
 // consecutive across a half-warp and reads of A are broadcasts.
-template <class T, int TM, int TN, int BK>
+// Grouped launches: blockIdx.x indexes the concatenated tile lists of
+// group[0..nprob) (sorted by tile_begin); otherwise it is a tile of args0.
+template <class T, int TM, int TN, int BK, bool kGroup>
 __global__ void __launch_bounds__(kThreads, 2)
-simt_contract(const GemmArgs args) {
+simt_contract(const GemmArgs args0, const SimtProblem* group, int nprob) {
   constexpr int BM = 16 * TM;
   constexpr int BN = 16 * TN;
+  int64_t tile = blockIdx.x;
+  // The contraction of this CTA: a shared-memory copy of its descriptor for
+  // grouped launches, the parameter space otherwise.
+  __shared__ GemmArgs group_args;
+  if constexpr (kGroup) {
+    int lo = 0, hi = nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (group[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+    }
+    tile -= group[lo].tile_begin;
+    if (threadIdx.x == 0) group_args = group[lo].g;
+    __syncthreads();
+  }
+  const GemmArgs& args = kGroup ? group_args : args0;
   constexpr int A_PER = BM * BK / kThreads;
   constexpr int B_PER = BN * BK / kThreads;
   static_assert(A_PER * kThreads == BM * BK, "A tile not divisible");
@@ -123,10 +140,9 @@ simt_contract(const GemmArgs args) {
   // Tile order: groups of 8 M-tiles sweep N so neighbouring CTAs share B.
   const int64_t tiles_m = (M + BM - 1) / BM;
   const int64_t tiles_n = (N + BN - 1) / BN;
-  const int64_t t = blockIdx.x;
+  const int64_t t = tile;
   constexpr int64_t G = 8;
-  const int64_t group = t / (G * tiles_n);
-  const int64_t first_m = group * G;
+  const int64_t first_m = (t / (G * tiles_n)) * G;
   const int64_t gsize = min(G, tiles_m - first_m);
   const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
   const int64_t tn = (t % (G * tiles_n)) / gsize;
@@ -257,11 +273,52 @@ cudaError_t launch(const GemmArgs& args, int splits, cudaStream_t stream) {
   if (tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   if (splits < 1 || splits > 65535) return cudaErrorInvalidConfiguration;
   const dim3 grid(static_cast<unsigned>(tiles), static_cast<unsigned>(splits));
-  simt_contract<T, TM, TN, BK><<<grid, kThreads, 0, stream>>>(args);
+  simt_contract<T, TM, TN, BK, false><<<grid, kThreads, 0, stream>>>(args, nullptr, 0);
+  return cudaGetLastError();
+}
+
+template <class T, int TM, int TN, int BK>
+cudaError_t launch_group(const SimtProblem* dev, int nprob, int64_t total_tiles,
+                         cudaStream_t stream) {
+  if (total_tiles <= 0) return cudaSuccess;
+  if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  GemmArgs none{};
+  simt_contract<T, TM, TN, BK, true><<<static_cast<unsigned>(total_tiles), kThreads, 0, stream>>>(
+      none, dev, nprob);
   return cudaGetLastError();
 }
 
 }  // namespace
+
+void simt_group_tile(int dtype, bool skinny, int* bm, int* bn) {
+  if (skinny) {
+    *bm = 128;
+    *bn = 16;
+    return;
+  }
+  int bk;
+  simt_tile(dtype, bm, bn, &bk);
+}
+
+cudaError_t launch_simt_group(int dtype, bool skinny, const SimtProblem* dev, int nprob,
+                              int64_t total_tiles, cudaStream_t stream) {
+  if (skinny) {
+    switch (dtype) {
+      case 0: return launch_group<float, 8, 1, 16>(dev, nprob, total_tiles, stream);
+      case 1: return launch_group<double, 8, 1, 16>(dev, nprob, total_tiles, stream);
+      case 2: return launch_group<float2, 8, 1, 16>(dev, nprob, total_tiles, stream);
+      case 3: return launch_group<double2, 8, 1, 16>(dev, nprob, total_tiles, stream);
+    }
+    return cudaErrorInvalidValue;
+  }
+  switch (dtype) {
+    case 0: return launch_group<float, 8, 8, 8>(dev, nprob, total_tiles, stream);
+    case 1: return launch_group<double, 8, 4, 8>(dev, nprob, total_tiles, stream);
+    case 2: return launch_group<float2, 4, 8, 8>(dev, nprob, total_tiles, stream);
+    case 3: return launch_group<double2, 4, 4, 8>(dev, nprob, total_tiles, stream);
+  }
+  return cudaErrorInvalidValue;
+}
 
 void simt_tile(int dtype, int* bm, int* bn, int* bk) {
   switch (dtype) {

@@ -9,18 +9,19 @@
 // any tensor in HBM:
 //
 //  1. Loader warps bring raw complex tiles into a ring of shared-memory
-//     stages.  A tile whose block-scatter blocks are regular (one uniform
-//     stride per bundle, the other unit stride) is fetched by ONE TMA
-//     instruction per operand (cp.async.bulk.tensor, 128-byte swizzle where
-//     the innermost run is K); other tiles are gathered element by element
-//     with cp.async through the scatter vectors (zero fill past the edges).
+//     stages.  Where the block-scatter blocks of an operand have unit stride
+//     (a bundle whose 16-element blocks are contiguous runs, or which is one
+//     uniform run), TMA fetches them: one cp.async.bulk.tensor per operand
+//     tile, or one per 16-row block, with the coordinates taken from the
+//     scatter vectors (128-byte swizzle where the innermost run is K).  Other
+//     operands are gathered element by element with cp.async through the
+//     scatter vectors (zero fill past the edges).
 //  2. Converter warps read a raw stage, build the 1M A rows [re, -im, ...]
-//     and [im, re, ...] for every complex row, split every value into TF32
-//     hi and lo parts (hi = rna(x), lo = rna(x - hi)) and store A hi/lo into
-//     TENSOR MEMORY with tcgen05.st (the 4x-expanded A never exists in shared
-//     or global memory) and B hi/lo into shared memory in the 128-byte-
-//     swizzled K-major layout the MMA descriptors read (the 1M B panel is the
-//     raw interleaved re/im data along K).
+//     and [im, re, ...] for every complex row, split every value into TF32 hi
+//     and lo parts and store A hi/lo into TENSOR MEMORY with tcgen05.st (the
+//     4x-expanded A never exists in shared or global memory) and B hi/lo into
+//     shared memory in the 128-byte-swizzled K-major layout the MMA
+//     descriptors read (the 1M B panel is the raw interleaved re/im data).
 //  3. One thread issues tcgen05.mma kind::tf32 (M = 128 real rows = 64 complex
 //     rows, N = 128 complex columns, K = 8).
 //
@@ -39,29 +40,40 @@
 //  t1m.h:425-426) across neighbouring lanes with one shuffle, applies
 //  alpha/beta and scatter-writes C.
 //
+// Persistence and grouping.  One CTA per SM loops over a list of output
+// tiles; the list may span many contractions of different shapes (a grouped
+// launch: one descriptor per contraction in global memory), so a batch of
+// uneven contractions runs as one launch.  All rings, chunk buffers and
+// accumulators carry over from tile to tile; the MMA of a tile waits until the
+// epilogue of the previous tile has read the accumulators.
+//
 // Synchronisation: mbarriers between loaders -> converters (raw ring),
 // converters -> MMA (operand stages), MMA -> converters (tcgen05.commit on
-// stage release and chunk completion).  Every wait is bounded
-// (ptx::mbar_wait); a timeout records an error code in a device word the
-// host checks, and the kernel leaves after freeing its tensor memory.
+// stage release, chunk completion and tile completion) and converters -> MMA
+// (chunk and accumulator release).  Every wait is bounded (ptx::mbar_wait); a
+// timeout records an error code in a device word the host checks, and the
+// kernel leaves after freeing its tensor memory.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "internal.h"
 #include "ptx.h"
 #include "t1m_capi.h"
+#include "tc.h"
 
 namespace t1m {
 namespace gb300 {
 namespace {
 
-constexpr int kTileMc = 64;     // complex rows per CTA (MMA M = 128 real rows)
-constexpr int kTileN = 128;     // complex columns per CTA (MMA N)
+constexpr int kTileMc = 64;     // complex rows per tile (MMA M = 128 real rows)
+constexpr int kTileN = 128;     // complex columns per tile (MMA N)
 constexpr int kStepK = 16;      // complex K per stage = 32 TF32 = one 128 B swizzle row
 constexpr int kRaw = 4;         // raw tile stages
 constexpr int kStages = 2;      // converted operand stages
@@ -95,20 +107,9 @@ enum : int {
   kErrEmptyWait = 2,
   kErrAccWait = 3,
   kErrChunkWait = 4,
-  kErrRawWait = 5
-};
-
-// How a raw operand tile is fetched, and hence its shared-memory layout.
-//   A: kMK  [k][m]   512 B per k, TMA (M unit stride)       / gather
-//      kKM  [m][k]   128 B rows, 128 B swizzle, TMA (K unit stride)
-//   B: kNK  [n][k]   128 B rows, 128 B swizzle, TMA (K unit stride) / gather
-//      kKN  [k][n]   1024 B per k, TMA (N unit stride)
-enum : int { kTmaMK = 0, kTmaKM = 1, kGatherMK = 2 };
-enum : int { kTmaNK = 0, kTmaKN = 1, kGatherNK = 2 };
-
-struct TmaMaps {
-  CUtensorMap a;
-  CUtensorMap b;
+  kErrRawWait = 5,
+  kErrAccEmptyWait = 6,
+  kErrDepWait = 7
 };
 
 __device__ __forceinline__ int64_t offs(const int64_t* v, int64_t u, int64_t i) {
@@ -167,17 +168,66 @@ __device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, ui
                : "memory");
 }
 
-template <int AMode, int BMode>
-__global__ void __launch_bounds__(kThreads, 1)
-tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
-  constexpr bool kTmaA = AMode != kGatherMK;
-  constexpr bool kTmaB = BMode != kGatherNK;
-  constexpr bool kGather = !kTmaA || !kTmaB;
-  // Arrivals per raw stage: one expect_tx arrive from the TMA thread, one
-  // cp.async completion arrive per gather thread.
-  constexpr uint32_t kRawArrivals = (kTmaA || kTmaB ? 1u : 0u) + (kGather ? kLoaders : 0u);
-  constexpr uint32_t kTmaBytes = (kTmaA ? kRawABytes : 0) + (kTmaB ? kRawBBytes : 0);
+// Position of one output tile in the tile list.
+struct TileRef {
+  const TcProblem* p;
+  int pi;
+  int64_t m0, n0, kb, ke, ksteps;
+};
 
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.s32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void red_release_add(int* p, int v) {
+  asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Converter warps only (256 threads): named barrier 1.
+__device__ __forceinline__ void converters_sync() {
+  asm volatile("bar.sync 1, 256;" ::: "memory");
+}
+
+// Tiles of problem p are numbered split-major; within a split, groups of 16
+// M-tiles sweep N so CTAs running together share B in L2.
+__device__ __forceinline__ TileRef locate(const TcProblem* single, const TcProblem* group,
+                                          int nprob, int64_t t) {
+  const TcProblem* p = single;
+  int lo = 0;
+  if (group) {
+    int hi = nprob - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (group[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
+    }
+    p = group + lo;
+  }
+  const int64_t lt = t - p->tile_begin;
+  const int64_t per_split = int64_t(p->tiles_m) * p->tiles_n;
+  const int64_t split = lt / per_split;
+  const int64_t r = lt % per_split;
+  constexpr int64_t G = 16;
+  const int64_t group_idx = r / (G * p->tiles_n);
+  const int64_t first_m = group_idx * G;
+  const int64_t gsize = min(G, int64_t(p->tiles_m) - first_m);
+  const int64_t tm = first_m + (r % (G * p->tiles_n)) % gsize;
+  const int64_t tn = (r % (G * p->tiles_n)) / gsize;
+  TileRef ref;
+  ref.p = p;
+  ref.pi = lo;
+  ref.m0 = tm * kTileMc;
+  ref.n0 = tn * kTileN;
+  ref.kb = split * p->g.k_per_split;
+  ref.ke = min(p->g.K, ref.kb + p->g.k_per_split);
+  ref.ksteps = (ref.ke - ref.kb + kStepK - 1) / kStepK;
+  return ref;
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* group, int nprob,
+                    int64_t total_tiles, int* done, int* err_flag) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const uint32_t base = (ptx::smem_u32(smem_raw) + 1023u) & ~1023u;
   uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
@@ -192,8 +242,9 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
   auto empty_bar = [&](int s) { return bars + 8u * (2 * kRaw + kStages + s); };
   auto chunk_full = [&](int b) { return bars + 8u * (2 * kRaw + 2 * kStages + b); };
   auto chunk_empty = [&](int b) { return bars + 8u * (2 * kRaw + 2 * kStages + 2 + b); };
-  const uint32_t acc_bar = bars + 8u * (2 * kRaw + 2 * kStages + 4);
-  const uint32_t tmem_slot = acc_bar + 8u;
+  const uint32_t acc_full = bars + 8u * (2 * kRaw + 2 * kStages + 4);
+  const uint32_t acc_empty = acc_full + 8u;
+  const uint32_t tmem_slot = acc_empty + 8u;
   volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(base_ptr + (tmem_slot - base));
 
   const int tid = threadIdx.x;
@@ -204,8 +255,10 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
     ptx::tmem_relinquish();
   }
   if (tid == 32) {
+    // Raw stages complete with one expect_tx arrival (TMA thread) plus one
+    // cp.async arrival per loader thread; both are issued for every stage.
     for (int r = 0; r < kRaw; ++r) {
-      ptx::mbar_init(raw_full(r), kRawArrivals);
+      ptx::mbar_init(raw_full(r), 1 + kLoaders);
       ptx::mbar_init(raw_empty(r), kConverters / 32);
     }
     for (int s = 0; s < kStages; ++s) {
@@ -216,125 +269,179 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
       ptx::mbar_init(chunk_full(b), 1);
       ptx::mbar_init(chunk_empty(b), kConverters / 32);
     }
-    ptx::mbar_init(acc_bar, 1);
+    ptx::mbar_init(acc_full, 1);
+    ptx::mbar_init(acc_empty, kConverters / 32);
     ptx::fence_mbar_init();
   }
-  if (tid == 64) {
-    if (kTmaA) ptx::tma_prefetch_desc(&maps.a);
-    if (kTmaB) ptx::tma_prefetch_desc(&maps.b);
+  if (tid == 64 && !group) {
+    if (single.amode != kAGather) ptx::tma_prefetch_desc(&single.map_a);
+    if (single.bmode != kBGather) ptx::tma_prefetch_desc(&single.map_b);
   }
   ptx::tc_fence_before();
   __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot_ptr;
 
-  const int64_t M = args.M, N = args.N;
-  // Split-K: this CTA row covers K range [kb, K) (kb a multiple of kStepK).
-  const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
-  const int64_t K = min(args.K, kb + args.k_per_split);
-  const int64_t tiles_m = (M + kTileMc - 1) / kTileMc;
-  const int64_t tiles_n = (N + kTileN - 1) / kTileN;
-  // Groups of 16 M-tiles sweep N so CTAs running together share B in L2.
-  constexpr int64_t G = 16;
-  const int64_t t = blockIdx.x;
-  const int64_t group = t / (G * tiles_n);
-  const int64_t first_m = group * G;
-  const int64_t gsize = min(G, tiles_m - first_m);
-  const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
-  const int64_t tn = (t % (G * tiles_n)) / gsize;
-  const int64_t m0 = tm * kTileMc, n0 = tn * kTileN;
-  const int64_t ksteps = (K - kb + kStepK - 1) / kStepK;
-
   if (warp == 0) {
     // ---------------------------------------------------------- MMA issue ---
     if (lane == 0) {
-      for (int64_t s = 0; s < ksteps; ++s) {
-        const int st = static_cast<int>(s % kStages);
-        const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
-        const int64_t c = s / kFold;
-        const int buf = static_cast<int>(c & 1);
-        const bool chunk_start = (s % kFold) == 0;
-        if (chunk_start && c >= 2 &&
-            !ptx::mbar_wait(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
-          record_error(err_flag, kErrChunkWait);
+      bool ok = true;
+      int64_t op_cnt = 0, chunk_cnt = 0, tile_cnt = 0;
+      for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++tile_cnt) {
+        const TileRef tr = locate(&single, group, nprob, t);
+        // The previous tile's epilogue must have read the accumulators.
+        if (tile_cnt > 0 && !ptx::mbar_wait(acc_empty, static_cast<uint32_t>((tile_cnt - 1) & 1))) {
+          record_error(err_flag, kErrAccEmptyWait);
+          ok = false;
           break;
         }
-        if (!ptx::mbar_wait(full_bar(st), ph)) {
-          record_error(err_flag, kErrFullWait);
-          break;
-        }
-        ptx::tc_fence_after();
-        const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
-        const uint32_t d_corr = tmem + kCorrCol;
-        const uint32_t a_hi = tmem + kAStageCol + 64u * st;
-        const uint32_t a_lo = a_hi + 32u;
-        const uint32_t b_hi = op0 + st * kOpBytes;
-        const uint32_t b_lo = b_hi + kBHalfBytes;
+        for (int64_t s = 0; s < tr.ksteps; ++s, ++op_cnt) {
+          const int st = static_cast<int>(op_cnt % kStages);
+          const uint32_t ph = static_cast<uint32_t>((op_cnt / kStages) & 1);
+          const bool chunk_start = (s % kFold) == 0;
+          if (chunk_start && s > 0) ++chunk_cnt;
+          const int buf = static_cast<int>(chunk_cnt & 1);
+          if (chunk_start && chunk_cnt >= 2 &&
+              !ptx::mbar_wait(chunk_empty(buf), static_cast<uint32_t>(((chunk_cnt - 2) >> 1) & 1))) {
+            record_error(err_flag, kErrChunkWait);
+            ok = false;
+            break;
+          }
+          if (!ptx::mbar_wait(full_bar(st), ph)) {
+            record_error(err_flag, kErrFullWait);
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
+          const uint32_t d_corr = tmem + kCorrCol;
+          const uint32_t a_hi = tmem + kAStageCol + 64u * st;
+          const uint32_t a_lo = a_hi + 32u;
+          const uint32_t b_hi = op0 + st * kOpBytes;
+          const uint32_t b_lo = b_hi + kBHalfBytes;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
-          const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
-          ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
-          ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
-          ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
+            const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
+            ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
+            ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
+            ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
+          }
+          ptx::mma_commit(empty_bar(st));
+          if ((s % kFold) == kFold - 1 || s == tr.ksteps - 1) ptx::mma_commit(chunk_full(buf));
         }
-        ptx::mma_commit(empty_bar(st));
-        if ((s % kFold) == kFold - 1 || s == ksteps - 1) ptx::mma_commit(chunk_full(buf));
+        if (!ok) break;
+        ++chunk_cnt;  // the next tile starts a fresh chunk
+        ptx::mma_commit(acc_full);
       }
-      // Signal the epilogue (also after an abort, so nobody waits forever),
-      // then make sure no MMA is still writing TMEM before it is freed.
-      ptx::mma_commit(acc_bar);
-      if (!ptx::mbar_wait(acc_bar, 0)) record_error(err_flag, kErrAccWait);
+      // Make sure no MMA is still writing TMEM before it is freed.
+      if (tile_cnt > 0 && !ptx::mbar_wait(acc_full, static_cast<uint32_t>((tile_cnt - 1) & 1)))
+        record_error(err_flag, kErrAccWait);
+      if (!ok) {
+        // Release the epilogue of a tile whose MMAs were cut short.
+        ptx::mma_commit(acc_full);
+      }
     }
     __syncwarp();
   } else if (tid < kConvBase) {
     // ------------------------------------------------------------ loaders ---
     const int lt = tid - kLoaderBase;  // 0..95
-    const float2* __restrict__ A = static_cast<const float2*>(args.A);
-    const float2* __restrict__ B = static_cast<const float2*>(args.B);
-    // Gather work of this thread: fixed rows / columns, K walked per stage.
-    for (int64_t s = 0; s < ksteps; ++s) {
-      const int r = static_cast<int>(s % kRaw);
-      const uint32_t ph = static_cast<uint32_t>((s / kRaw) & 1);
-      const int64_t k0 = kb + s * kStepK;
-      if (kGather || lt == 0) {
-        if (!ptx::mbar_wait(raw_empty(r), ph ^ 1u)) {
-          record_error(err_flag, kErrRawWait);
-          break;
+    int64_t raw_cnt = 0;
+    for (int64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
+      const TileRef tr = locate(&single, group, nprob, t);
+      const TcProblem* p = tr.p;
+      const GemmArgs& g = p->g;
+      const float2* __restrict__ A = static_cast<const float2*>(g.A);
+      const float2* __restrict__ B = static_cast<const float2*>(g.B);
+      const int amode = p->amode, bmode = p->bmode;
+      // Row offsets of the four 16-row A blocks (block TMA), per tile.
+      int c0a[4] = {0, 0, 0, 0};
+      if (amode == kAMK16 && lt == 0) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const int64_t m = tr.m0 + 16 * j;
+          c0a[j] = m < g.M ? static_cast<int>(2 * offs(g.rsA, g.uA_m, m)) : 0;
         }
       }
-      if ((kTmaA || kTmaB) && lt == 0) {
-        ptx::mbar_arrive_expect_tx(raw_full(r), kTmaBytes);
-        if (AMode == kTmaMK)
-          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * m0), static_cast<int>(k0), raw_full(r));
-        if (AMode == kTmaKM)
-          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * k0), static_cast<int>(m0), raw_full(r));
-        if (BMode == kTmaNK)
-          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * k0), static_cast<int>(n0), raw_full(r));
-        if (BMode == kTmaKN)
-          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * n0), static_cast<int>(k0), raw_full(r));
+      // Tiles fetched entirely by TMA need only the TMA thread; the other
+      // loader threads skip them (the TMA thread arrives on their behalf).
+      const bool gathering = amode == kAGather || bmode == kBGather;
+      if (!gathering && lt != 0) {
+        raw_cnt += tr.ksteps;
+        continue;
       }
-      if (kGather) {
-        if (AMode == kGatherMK) {
+      bool stop = false;
+      if (done && p->dep >= 0) {
+        // This problem reads the C of problem p->dep: wait (bounded) until all
+        // of its tiles are written, then order those generic-proxy writes
+        // before this thread's TMA / cp.async reads.
+        const int* ctr = done + p->dep;
+        if (ld_acquire(ctr) < p->dep_tiles) {
+          const long long t0 = clock64();
+          while (ld_acquire(ctr) < p->dep_tiles) {
+            __nanosleep(200);
+            if (clock64() - t0 > ptx::kSpinBudget) {
+              record_error(err_flag, kErrDepWait);
+              stop = true;
+              break;
+            }
+          }
+        }
+        asm volatile("fence.proxy.async.global;" ::: "memory");
+      }
+      for (int64_t s = 0; s < tr.ksteps && !stop; ++s, ++raw_cnt) {
+        const int r = static_cast<int>(raw_cnt % kRaw);
+        const uint32_t ph = static_cast<uint32_t>((raw_cnt / kRaw) & 1);
+        const int64_t k0 = tr.kb + s * kStepK;
+        if (!ptx::mbar_wait(raw_empty(r), ph ^ 1u)) {
+          record_error(err_flag, kErrRawWait);
+          stop = true;
+          break;
+        }
+        if (lt == 0) {
+          const uint32_t bytes = (amode != kAGather ? kRawABytes : 0) +
+                                 (bmode != kBGather ? kRawBBytes : 0);
+          ptx::mbar_arrive_expect_tx(raw_full(r), bytes);
+          if (amode == kAMK)
+            ptx::tma_load_2d(raw_a(r), &p->map_a, static_cast<int>(2 * tr.m0), static_cast<int>(k0), raw_full(r));
+          if (amode == kAMK16)
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              ptx::tma_load_2d(raw_a(r) + 2048u * j, &p->map_a, c0a[j], static_cast<int>(k0), raw_full(r));
+          if (amode == kAKM)
+            ptx::tma_load_2d(raw_a(r), &p->map_a, static_cast<int>(2 * offs(g.csA, g.uA_k, k0)),
+                             static_cast<int>(tr.m0), raw_full(r));
+          if (bmode == kBNK)
+            ptx::tma_load_2d(raw_b(r), &p->map_b, static_cast<int>(2 * offs(g.rsB, g.uB_k, k0)),
+                             static_cast<int>(tr.n0), raw_full(r));
+          if (bmode == kBKN)
+            ptx::tma_load_2d(raw_b(r), &p->map_b, static_cast<int>(2 * tr.n0), static_cast<int>(k0), raw_full(r));
+          if (!gathering) {
+            ptx::mbar_arrive_count(raw_full(r), kLoaders);
+            continue;
+          }
+        }
+        if (amode == kAGather) {
           // [k][m]: consecutive threads walk m (coalesced where M is unit stride).
           for (int e = lt; e < kTileMc * kStepK; e += kLoaders) {
             const int m = e % kTileMc, k = e / kTileMc;
-            const bool ok = (m0 + m < M) && (k0 + k < K);
-            const float2* src = ok ? A + offs(args.rsA, args.uA_m, m0 + m) + offs(args.csA, args.uA_k, k0 + k) : A;
-            ptx::cp_async_8(raw_a(r) + static_cast<uint32_t>(k * 512 + m * 8), src, ok ? 8u : 0u);
+            const bool in = (tr.m0 + m < g.M) && (k0 + k < tr.ke);
+            const float2* src = in ? A + offs(g.rsA, g.uA_m, tr.m0 + m) + offs(g.csA, g.uA_k, k0 + k) : A;
+            ptx::cp_async_8(raw_a(r) + static_cast<uint32_t>(k * 512 + m * 8), src, in ? 8u : 0u);
           }
         }
-        if (BMode == kGatherNK) {
+        if (bmode == kBGather) {
           // [n][k] swizzled: consecutive threads walk k.
           for (int e = lt; e < kTileN * kStepK; e += kLoaders) {
             const int k = e % kStepK, n = e / kStepK;
-            const bool ok = (n0 + n < N) && (k0 + k < K);
-            const float2* src = ok ? B + offs(args.rsB, args.uB_k, k0 + k) + offs(args.csB, args.uB_n, n0 + n) : B;
-            ptx::cp_async_8(raw_b(r) + swz128(n, k), src, ok ? 8u : 0u);
+            const bool in = (tr.n0 + n < g.N) && (k0 + k < tr.ke);
+            const float2* src = in ? B + offs(g.rsB, g.uB_k, k0 + k) + offs(g.csB, g.uB_n, tr.n0 + n) : B;
+            ptx::cp_async_8(raw_b(r) + swz128(n, k), src, in ? 8u : 0u);
           }
         }
         ptx::cp_async_arrive_noinc(raw_full(r));
       }
+      if (stop) break;
     }
   } else {
     // -------------------------------------------- converters, fold, epilogue ---
@@ -345,16 +452,8 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
     const int ci = rho >> 1;         // complex row in the tile
     const int part = rho & 1;        // 0: real row "re", 1: "im"
     const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
-    const bool conjA = args.flags & kFlagConjA;
-    const bool conjB = args.flags & kFlagConjB;
-    const bool row_ok = (m0 + ci) < M;
 
     float master[64];
-#pragma unroll
-    for (int j = 0; j < 64; ++j) master[j] = 0.f;
-
-    // Fold chunk accumulator at column `col` into the FP32 master registers
-    // (round-to-nearest adds): this thread's lane, 64 columns.
     auto fold_from = [&](uint32_t col) {
 #pragma unroll
       for (int cc = 0; cc < 4; ++cc) {
@@ -366,154 +465,174 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
       }
     };
 
-    // Loop-invariant shared-memory offsets of this thread's raw reads and
-    // operand writes.
-    uint32_t aoff[8];
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-      aoff[j] = (AMode == kTmaKM) ? swz128(ci, 8 * wg + 2 * (j >> 1))
-                                  : static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8);
-    uint32_t bsrc[4], boff[4][2];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int id = pt + 256 * j;
-      if (BMode == kTmaKN) {
-        const int k = id >> 6, n = 2 * (id & 63);
-        bsrc[j] = static_cast<uint32_t>(k * 1024 + n * 8);
-        boff[j][0] = swz128(n, k);
-        boff[j][1] = swz128(n + 1, k);
-      } else {
-        const int n = id >> 3, kp = id & 7;
-        bsrc[j] = swz128(n, 2 * kp);
-        boff[j][0] = bsrc[j];
-        boff[j][1] = 0;
-      }
-    }
-
     bool ok = true;
-    int r = 0, st = 0;
-    uint32_t rph = 0, ph = 0;
-    for (int64_t s = 0; s < ksteps; ++s) {
-      if (!ptx::mbar_wait(raw_full(r), rph)) {
-        record_error(err_flag, kErrRawWait);
-        ok = false;
-        break;
-      }
-      // A: eight complex k (this half of the step) of complex row ci.
-      const uint32_t ra = raw_a(r), rb = raw_b(r);
-      float2 av[8];
-      if (AMode == kTmaKM) {
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          const float4 v = lds128(ra + aoff[2 * j]);
-          av[2 * j] = make_float2(v.x, v.y);
-          av[2 * j + 1] = make_float2(v.z, v.w);
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) av[j] = lds64(ra + aoff[j]);
-      }
-      // B: four 16-byte pieces (two complex each) of the raw tile.
-      float4 bv[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
-      __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(raw_empty(r));
+    int64_t raw_cnt = 0, op_cnt = 0, chunk_cnt = 0, tile_cnt = 0;
+    for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++tile_cnt) {
+      const TileRef tr = locate(&single, group, nprob, t);
+      const TcProblem* p = tr.p;
+      const GemmArgs& g = p->g;
+      const int amode = p->amode, bmode = p->bmode;
+      const bool conjA = g.flags & kFlagConjA;
+      const bool conjB = g.flags & kFlagConjB;
+      const bool row_ok = (tr.m0 + ci) < g.M;
 
-      if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
-        record_error(err_flag, kErrEmptyWait);
-        ok = false;
-        break;
-      }
-      ptx::tc_fence_after();
-      // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
-      uint32_t hi[16], lo[16];
+      // Shared-memory offsets of this thread's raw reads and operand writes.
+      uint32_t aoff[8];
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
-        float2 v = av[j];
-        if (conjA) v.y = -v.y;
-        if (!row_ok) v = make_float2(0.f, 0.f);
-        const float x0 = part ? v.y : v.x;
-        const float x1 = part ? v.x : -v.y;
-        const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
-        hi[2 * j] = s0.hi;
-        lo[2 * j] = s0.lo;
-        hi[2 * j + 1] = s1.hi;
-        lo[2 * j + 1] = s1.lo;
+        if (amode == kAKM)
+          aoff[j] = swz128(ci, 8 * wg + 2 * (j >> 1));
+        else if (amode == kAMK16)
+          aoff[j] = static_cast<uint32_t>((ci >> 4) * 2048 + (8 * wg + j) * 128 + (ci & 15) * 8);
+        else
+          aoff[j] = static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8);
       }
-      const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 16u * wg;
-      ptx::tmem_st16(a_col, hi);
-      ptx::tmem_st16(a_col + 32u, lo);
-      // B -> shared memory (swizzled K-major hi and lo tiles).
-      const uint32_t ob = op0 + st * kOpBytes;
+      uint32_t bsrc[4], boff[4][2];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        float4 v = bv[j];
-        if (conjB) {
-          v.y = -v.y;
-          v.w = -v.w;
-        }
-        const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
-        const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
-        if (BMode == kTmaKN) {
-          sts64(ob + boff[j][0], r0.hi, i0.hi);
-          sts64(ob + boff[j][1], r1.hi, i1.hi);
-          sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
-          sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
+        const int id = pt + 256 * j;
+        if (bmode == kBKN) {
+          const int k = id >> 6, n = 2 * (id & 63);
+          bsrc[j] = static_cast<uint32_t>(k * 1024 + n * 8);
+          boff[j][0] = swz128(n, k);
+          boff[j][1] = swz128(n + 1, k);
         } else {
-          sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
-          sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+          const int n = id >> 3, kp = id & 7;
+          bsrc[j] = swz128(n, 2 * kp);
+          boff[j][0] = bsrc[j];
+          boff[j][1] = 0;
         }
       }
-      ptx::tmem_wait_st();
-      ptx::fence_proxy_async_smem();
-      ptx::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(full_bar(st));
+#pragma unroll
+      for (int j = 0; j < 64; ++j) master[j] = 0.f;
 
-      // Fold the previous chunk once the first stage of the next is queued.
-      if ((s % kFold) == 0 && s >= kFold) {
-        const int64_t c = s / kFold - 1;
-        const int buf = static_cast<int>(c & 1);
-        if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
-          record_error(err_flag, kErrChunkWait);
+      const int64_t chunk_base = chunk_cnt;
+      for (int64_t s = 0; s < tr.ksteps; ++s, ++raw_cnt, ++op_cnt) {
+        const int r = static_cast<int>(raw_cnt % kRaw);
+        const uint32_t rph = static_cast<uint32_t>((raw_cnt / kRaw) & 1);
+        const int st = static_cast<int>(op_cnt % kStages);
+        const uint32_t ph = static_cast<uint32_t>((op_cnt / kStages) & 1);
+        if (!ptx::mbar_wait(raw_full(r), rph)) {
+          record_error(err_flag, kErrRawWait);
+          ok = false;
+          break;
+        }
+        const uint32_t ra = raw_a(r), rb = raw_b(r);
+        float2 av[8];
+        if (amode == kAKM) {
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            const float4 v = lds128(ra + aoff[2 * j]);
+            av[2 * j] = make_float2(v.x, v.y);
+            av[2 * j + 1] = make_float2(v.z, v.w);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 8; ++j) av[j] = lds64(ra + aoff[j]);
+        }
+        float4 bv[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(raw_empty(r));
+
+        if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
+          record_error(err_flag, kErrEmptyWait);
           ok = false;
           break;
         }
         ptx::tc_fence_after();
-        fold_from(buf ? kChunkCol1 : kChunkCol0);
+        // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
+        uint32_t hi[16], lo[16];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          float2 v = av[j];
+          if (conjA) v.y = -v.y;
+          if (!row_ok) v = make_float2(0.f, 0.f);
+          const float x0 = part ? v.y : v.x;
+          const float x1 = part ? v.x : -v.y;
+          const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
+          hi[2 * j] = s0.hi;
+          lo[2 * j] = s0.lo;
+          hi[2 * j + 1] = s1.hi;
+          lo[2 * j + 1] = s1.lo;
+        }
+        const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 16u * wg;
+        ptx::tmem_st16(a_col, hi);
+        ptx::tmem_st16(a_col + 32u, lo);
+        // B -> shared memory (swizzled K-major hi and lo tiles).
+        const uint32_t ob = op0 + st * kOpBytes;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          float4 v = bv[j];
+          if (conjB) {
+            v.y = -v.y;
+            v.w = -v.w;
+          }
+          const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
+          const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
+          if (bmode == kBKN) {
+            sts64(ob + boff[j][0], r0.hi, i0.hi);
+            sts64(ob + boff[j][1], r1.hi, i1.hi);
+            sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
+            sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
+          } else {
+            sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
+            sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+          }
+        }
+        ptx::tmem_wait_st();
+        ptx::fence_proxy_async_smem();
         ptx::tc_fence_before();
         __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(chunk_empty(buf));
-      }
-      if (++r == kRaw) {
-        r = 0;
-        rph ^= 1u;
-      }
-      if (++st == kStages) {
-        st = 0;
-        ph ^= 1u;
-      }
-    }
+        if (lane == 0) ptx::mbar_arrive(full_bar(st));
 
-    // ---------------------------------------------------------- epilogue ---
-    if (!ptx::mbar_wait(acc_bar, 0)) {
-      record_error(err_flag, kErrAccWait);
-      ok = false;
-    }
-    ptx::tc_fence_after();
-    if (ok) {
-      // The last chunk was never folded in the loop; then add the corrections.
-      const int64_t c_last = (ksteps - 1) / kFold;
-      fold_from((c_last & 1) ? kChunkCol1 : kChunkCol0);
+        // Fold the previous chunk once the first stage of the next is queued.
+        if ((s % kFold) == 0 && s >= kFold) {
+          const int64_t c = chunk_base + s / kFold - 1;
+          const int buf = static_cast<int>(c & 1);
+          if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
+            record_error(err_flag, kErrChunkWait);
+            ok = false;
+            break;
+          }
+          ptx::tc_fence_after();
+          fold_from(buf ? kChunkCol1 : kChunkCol0);
+          ptx::tc_fence_before();
+          __syncwarp();
+          if (lane == 0) ptx::mbar_arrive(chunk_empty(buf));
+        }
+      }
+      if (!ok) break;
+
+      // -------------------------------------------------------- epilogue ---
+      if (!ptx::mbar_wait(acc_full, static_cast<uint32_t>(tile_cnt & 1))) {
+        record_error(err_flag, kErrAccWait);
+        ok = false;
+        break;
+      }
+      ptx::tc_fence_after();
+      // The last chunk of the tile was not folded in the loop; then the
+      // corrections.  After these reads the accumulators are free again.
+      const int64_t c_last = chunk_base + (tr.ksteps - 1) / kFold;
+      const int buf_last = static_cast<int>(c_last & 1);
+      fold_from(buf_last ? kChunkCol1 : kChunkCol0);
       fold_from(kCorrCol);
-      const bool accumulate = args.flags & kFlagAccumulate;
-      const bool beta_zero = args.flags & kFlagBetaZero;
-      const float ar = (float)args.alpha[0], ai = (float)args.alpha[1];
-      const float br = (float)args.beta[0], bi = (float)args.beta[1];
-      float2* __restrict__ Cp =
-          static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
-      const int64_t rowC = row_ok ? offs(args.rsC, args.uC_m, m0 + ci) : 0;
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        ptx::mbar_arrive(chunk_empty(buf_last));
+        ptx::mbar_arrive(acc_empty);
+      }
+      chunk_cnt = c_last + 1;
+
+      const bool accumulate = g.flags & kFlagAccumulate;
+      const bool beta_zero = g.flags & kFlagBetaZero;
+      const float ar = (float)g.alpha[0], ai = (float)g.alpha[1];
+      const float br = (float)g.beta[0], bi = (float)g.beta[1];
+      const int64_t split = tr.kb / g.k_per_split;
+      float2* __restrict__ Cp = static_cast<float2*>(g.C) + split * g.c_split_stride;
+      const int64_t rowC = row_ok ? offs(g.rsC, g.uC_m, tr.m0 + ci) : 0;
 #pragma unroll
       for (int j = 0; j < 32; ++j) {
         const float v0 = master[2 * j], v1 = master[2 * j + 1];
@@ -522,20 +641,28 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
         const int col = wg * 64 + 2 * j + part;
         const float re = part ? recv : v0;
         const float im = part ? v1 : recv;
-        const int64_t n = n0 + col;
-        if (row_ok && n < N) {
-          float2* p = Cp + rowC + offs(args.csC, args.uC_n, n);
-          const float tr = ar * re - ai * im;
-          const float ti = ar * im + ai * re;
+        const int64_t n = tr.n0 + col;
+        if (row_ok && n < g.N) {
+          float2* pc = Cp + rowC + offs(g.csC, g.uC_n, n);
+          const float tr_ = ar * re - ai * im;
+          const float ti_ = ar * im + ai * re;
           if (accumulate) {
-            const float2 o = *p;
-            *p = make_float2(o.x + tr, o.y + ti);
+            const float2 o = *pc;
+            *pc = make_float2(o.x + tr_, o.y + ti_);
           } else if (beta_zero) {
-            *p = make_float2(tr, ti);
+            *pc = make_float2(tr_, ti_);
           } else {
-            const float2 o = *p;
-            *p = make_float2(tr + (br * o.x - bi * o.y), ti + (br * o.y + bi * o.x));
+            const float2 o = *pc;
+            *pc = make_float2(tr_ + (br * o.x - bi * o.y), ti_ + (br * o.y + bi * o.x));
           }
+        }
+      }
+      if (done) {
+        // Publish the tile: every converter's stores, then one release-add.
+        converters_sync();
+        if (pt == 0) {
+          __threadfence();
+          red_release_add(done + tr.pi, 1);
         }
       }
     }
@@ -569,7 +696,7 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 2-D map over a complex64 matrix viewed as floats: dim0 = 2*inner (unit
+// 2-D map over complex64 data viewed as floats: dim0 = 2*inner floats (unit
 // stride), dim1 = outer with `outer_stride` complex elements.
 bool make_map(CUtensorMap* map, const void* base, int64_t inner, int64_t outer,
               int64_t outer_stride, uint32_t box_inner_floats, uint32_t box_outer, bool swizzle) {
@@ -577,7 +704,8 @@ bool make_map(CUtensorMap* map, const void* base, int64_t inner, int64_t outer,
   if (!fn) return false;
   if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
   if (outer > 1 && ((outer_stride * 8) % 16 != 0 || outer_stride <= 0)) return false;
-  if (2 * inner >= (int64_t(1) << 31) || outer >= (int64_t(1) << 31)) return false;
+  if (2 * inner >= (int64_t(1) << 31) || outer >= (int64_t(1) << 31) || inner <= 0 || outer <= 0)
+    return false;
   cuuint64_t dims[2] = {static_cast<cuuint64_t>(2 * inner), static_cast<cuuint64_t>(outer)};
   cuuint64_t strides[1] = {static_cast<cuuint64_t>(outer > 1 ? outer_stride * 8 : 16)};
   cuuint32_t box[2] = {box_inner_floats, box_outer};
@@ -589,29 +717,21 @@ bool make_map(CUtensorMap* map, const void* base, int64_t inner, int64_t outer,
   return r == CUDA_SUCCESS;
 }
 
-template <int AMode, int BMode>
-cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
-                         int* err_flag, dim3 tiles) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc3xtf32_contract<AMode, BMode>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
+// Every 16-aligned block of the scatter vector is a unit-stride run starting
+// at an even offset (16-byte aligned complex64): the block-scatter condition
+// for one TMA box per block.
+bool unit_blocks16(const std::vector<int64_t>& v, int64_t n) {
+  for (int64_t b = 0; b < n; b += 16) {
+    if (v[b] & 1) return false;
+    const int64_t e = std::min<int64_t>(n, b + 16);
+    for (int64_t i = b + 1; i < e; ++i)
+      if (v[i] != v[b] + (i - b)) return false;
   }
-  tc3xtf32_contract<AMode, BMode><<<tiles, kThreads, kSmemBytes, stream>>>(args, maps, err_flag);
-  return cudaGetLastError();
+  return true;
 }
 
-template <int AMode>
-cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
-                     int* err_flag, dim3 tiles) {
-  switch (bmode) {
-    case kTmaNK: return launch_modes<AMode, kTmaNK>(args, maps, stream, err_flag, tiles);
-    case kTmaKN: return launch_modes<AMode, kTmaKN>(args, maps, stream, err_flag, tiles);
-    default: return launch_modes<AMode, kGatherNK>(args, maps, stream, err_flag, tiles);
-  }
-}
+std::mutex g_attr_mutex;
+bool g_attr_set = false;
 
 }  // namespace
 
@@ -626,6 +746,78 @@ bool tc_supported(int method, int dtype, const HostPlan& plan) {
   return method == T1M_METHOD_TC_3XTF32 && dtype == T1M_COMPLEX64;
 }
 
+bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p) {
+  std::memset(static_cast<void*>(p), 0, sizeof(*p));
+  p->g = g;
+  p->tiles_m = static_cast<int32_t>((g.M + kTileMc - 1) / kTileMc);
+  p->tiles_n = static_cast<int32_t>((g.N + kTileN - 1) / kTileN);
+  p->splits = splits;
+  if (splits < 1 || (splits > 1 && g.k_per_split % kStepK != 0)) return false;
+  if (g.M >= (int64_t(1) << 31) / kTileMc || g.N >= (int64_t(1) << 31) / kTileN) return false;
+  // A: TMA over a uniform 2-D view, TMA per unit-stride 16-row block, or gather.
+  p->amode = kAGather;
+  if (plan.uA_m == 1 && plan.uA_k >= 0 &&
+      make_map(&p->map_a, g.A, g.M, g.K, plan.uA_k, 2 * kTileMc, kStepK, false))
+    p->amode = kAMK;
+  else if (plan.uA_k == 1 && plan.uA_m >= 0 &&
+           make_map(&p->map_a, g.A, g.K, g.M, plan.uA_m, 2 * kStepK, kTileMc, true))
+    p->amode = kAKM;
+  else if (plan.uA_k >= 0 && unit_blocks16(plan.rsA, g.M) &&
+           make_map(&p->map_a, g.A, plan.spanA, g.K, plan.uA_k, 32, kStepK, false))
+    p->amode = kAMK16;
+  else if (plan.uA_m >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.csA, g.K) &&
+           make_map(&p->map_a, g.A, plan.spanA, g.M, plan.uA_m, 2 * kStepK, kTileMc, true))
+    p->amode = kAKM;
+  // B: TMA over a uniform 2-D view or per unit-stride 16-element K block, or gather.
+  p->bmode = kBGather;
+  if (plan.uB_k == 1 && plan.uB_n >= 0 &&
+      make_map(&p->map_b, g.B, g.K, g.N, plan.uB_n, 2 * kStepK, kTileN, true))
+    p->bmode = kBNK;
+  else if (plan.uB_n == 1 && plan.uB_k >= 0 &&
+           make_map(&p->map_b, g.B, g.N, g.K, plan.uB_k, 2 * kTileN, kStepK, false))
+    p->bmode = kBKN;
+  else if (plan.uB_n >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.rsB, g.K) &&
+           make_map(&p->map_b, g.B, plan.spanB, g.N, plan.uB_n, 2 * kStepK, kTileN, true))
+    p->bmode = kBNK;
+  return true;
+}
+
+int64_t tc_problem_tiles(const TcProblem& p) {
+  return int64_t(p.tiles_m) * p.tiles_n * p.splits;
+}
+
+cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_group, int nprob,
+                                 int64_t total_tiles, int num_sms, int* done,
+                                 cudaStream_t stream, int* err_flag) {
+  {
+    std::lock_guard<std::mutex> lock(g_attr_mutex);
+    if (!g_attr_set) {
+      cudaError_t e = cudaFuncSetAttribute(tc3xtf32_persistent,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+      if (e != cudaSuccess) return e;
+      g_attr_set = true;
+    }
+  }
+  if (total_tiles <= 0) return cudaSuccess;
+  const int64_t grid = std::min<int64_t>(total_tiles, std::max(1, num_sms));
+  TcProblem dummy;
+  if (!single) {
+    std::memset(static_cast<void*>(&dummy), 0, sizeof(dummy));
+    single = &dummy;
+  }
+  if (done) {
+    // Tiles wait on tiles of other CTAs: all CTAs must be resident.
+    void* params[] = {const_cast<TcProblem*>(single), &dev_group, &nprob, &total_tiles, &done,
+                      &err_flag};
+    return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(tc3xtf32_persistent),
+                                       dim3(static_cast<unsigned>(grid)), dim3(kThreads), params,
+                                       kSmemBytes, stream);
+  }
+  tc3xtf32_persistent<<<static_cast<unsigned>(grid), kThreads, kSmemBytes, stream>>>(
+      *single, dev_group, nprob, total_tiles, done, err_flag);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err) {
@@ -634,35 +826,16 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     *err = "tensor-core method not available for this dtype";
     return cudaErrorNotSupported;
   }
-  const int64_t tiles = ((args.M + kTileMc - 1) / kTileMc) * ((args.N + kTileN - 1) / kTileN);
-  if (tiles == 0) return cudaSuccess;
-  if (tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  // Operand fetch modes: TMA where the matricised operand is a regular 2-D
-  // strided matrix with one unit-stride direction, gather otherwise.
-  TmaMaps maps;
-  std::memset(&maps, 0, sizeof(maps));
-  int amode = kGatherMK, bmode = kGatherNK;
-  if (plan.uA_m == 1 && plan.uA_k >= 0 &&
-      make_map(&maps.a, args.A, args.M, args.K, plan.uA_k, 2 * kTileMc, kStepK, false))
-    amode = kTmaMK;
-  else if (plan.uA_k == 1 && plan.uA_m >= 0 &&
-           make_map(&maps.a, args.A, args.K, args.M, plan.uA_m, 2 * kStepK, kTileMc, true))
-    amode = kTmaKM;
-  if (plan.uB_k == 1 && plan.uB_n >= 0 &&
-      make_map(&maps.b, args.B, args.K, args.N, plan.uB_n, 2 * kStepK, kTileN, true))
-    bmode = kTmaNK;
-  else if (plan.uB_n == 1 && plan.uB_k >= 0 &&
-           make_map(&maps.b, args.B, args.N, args.K, plan.uB_k, 2 * kTileN, kStepK, false))
-    bmode = kTmaKN;
-  cudaError_t e;
-  if (splits < 1 || splits > 65535 || (splits > 1 && args.k_per_split % kStepK != 0))
-    return cudaErrorInvalidConfiguration;
-  const dim3 nt(static_cast<unsigned>(tiles), static_cast<unsigned>(splits));
-  switch (amode) {
-    case kTmaMK: e = launch_b<kTmaMK>(bmode, args, maps, stream, err_flag, nt); break;
-    case kTmaKM: e = launch_b<kTmaKM>(bmode, args, maps, stream, err_flag, nt); break;
-    default: e = launch_b<kGatherMK>(bmode, args, maps, stream, err_flag, nt); break;
-  }
+  if (args.M == 0 || args.N == 0) return cudaSuccess;
+  TcProblem p;
+  if (!tc_prepare(args, plan, splits, &p)) return cudaErrorInvalidConfiguration;
+  p.tile_begin = 0;
+  int dev = 0, sms = 152;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  p.dep = -1;
+  const cudaError_t e =
+      tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
   if (e == cudaSuccess) *kernels = 1;
   return e;
 }

@@ -1,0 +1,55 @@
+// Problem descriptor of the persistent tensor-core kernel (tc.cu), shared with
+// the grouped-launch host code (grouped.cu).
+#pragma once
+
+#include <cuda.h>
+
+#include <cstdint>
+#include <string>
+
+#include "internal.h"
+
+namespace t1m {
+namespace gb300 {
+
+// Operand fetch modes (see tc.cu).
+//   A: gather [k][m];  MK: one TMA box [k][64 m] (M unit stride, uniform K);
+//      MK16: four TMA boxes [16 k][16 m], one per unit-stride 16-row block;
+//      KM: one TMA box [64 m][16 k] with 128 B swizzle (K unit stride, or
+//      unit-stride 16-element K blocks and uniform M)
+//   B: gather [n][k] swizzled;  NK: one TMA box [128 n][16 k] with 128 B
+//      swizzle (K unit stride, or unit-stride 16-element K blocks);
+//      KN: one TMA box [16 k][128 n] (N unit stride)
+enum : int32_t { kAGather = 0, kAMK = 1, kAMK16 = 2, kAKM = 3 };
+enum : int32_t { kBGather = 0, kBNK = 1, kBKN = 2 };
+
+struct alignas(64) TcProblem {
+  CUtensorMap map_a;
+  CUtensorMap map_b;
+  GemmArgs g;
+  int32_t amode, bmode;
+  int32_t tiles_m, tiles_n, splits;
+  // Grouped launches: problem whose C this one reads (-1: none), and its tile
+  // count; the loaders of this problem wait until that many of its tiles have
+  // been written.
+  int32_t dep;
+  int32_t dep_tiles;
+  int32_t reserved;
+  int64_t tile_begin;  // first tile of this problem in the launch's tile list
+};
+
+// Fill a descriptor (fetch modes, tensor maps, tile counts).  False if the
+// problem cannot run on this kernel.
+bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p);
+int64_t tc_problem_tiles(const TcProblem& p);
+// One persistent launch over `total_tiles` tiles of `single` (dev_group null)
+// or of the device array dev_group[0..nprob) (sorted by tile_begin, every
+// dependency's tiles before its dependents').  `done` (grouped launches with
+// dependencies) holds one zeroed tile-completion counter per problem; such
+// launches are cooperative so all CTAs are resident.
+cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_group, int nprob,
+                                 int64_t total_tiles, int num_sms, int* done,
+                                 cudaStream_t stream, int* err_flag);
+
+}  // namespace gb300
+}  // namespace t1m

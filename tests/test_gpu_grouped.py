@@ -1,0 +1,132 @@
+"""Grouped batches (t1m_group_*): results equal the same contractions issued
+one call at a time, and the FP64 oracle (gpu)."""
+import numpy as np
+import pytest
+
+from oracle import numpy_oracle as no
+
+pytestmark = pytest.mark.gpu
+
+
+def _rand(rng, shape, dt, scale=1.0):
+    x = rng.normal(0, scale, shape) + 1j * rng.normal(0, scale, shape)
+    return x.astype(dt)
+
+
+def _sweep_items(torch, t1m, rng, n, choices, st_choices, dt=np.complex64):
+    """Config-4-style updates: xay,asb->xsyb then xsyb,ytb->xst."""
+    items, host = [], []
+    for _ in range(n):
+        x, y, a, b = (int(v) for v in rng.choice(choices, 4))
+        s, t = (int(v) for v in rng.choice(st_choices, 2))
+        bond = np.sqrt(a)
+        X1 = _rand(rng, (x, a, y), dt, 1 / np.sqrt(bond))
+        X2 = _rand(rng, (a, s, b), dt, 1 / np.sqrt(bond))
+        X3 = _rand(rng, (y, t, b), dt, 1 / np.sqrt(bond))
+        g1, g2, g3 = (torch.from_numpy(v.copy()).cuda() for v in (X1, X2, X3))
+        r1 = torch.zeros((x, s, y, b), dtype=g1.dtype, device="cuda")
+        out = torch.zeros((x, s, t), dtype=g1.dtype, device="cuda")
+        v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+        i1 = len(items)
+        items.append((1.0, v(g1), "xay", v(g2), "asb", 0.0, v(r1), "xsyb", -1))
+        items.append((1.0, v(r1), "xsyb", v(g3), "ytb", 0.0, v(out), "xst", i1))
+        host.append((X1, X2, X3, r1, out, (g1, g2, g3)))
+    return items, host
+
+
+@pytest.mark.parametrize("graph", [True, False])
+@pytest.mark.parametrize("autotune", [False, True])
+def test_sweep_batch_matches_fp64(ctx, torch_cuda, graph, autotune, tmp_path, monkeypatch):
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    monkeypatch.setenv("T1M_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    rng = np.random.default_rng(31)
+    items, host = _sweep_items(torch, t1m, rng, 6, [16, 32, 48], [2, 4])
+    grp = t1m.Group(items, ctx=ctx, graph=graph, autotune=autotune)
+    for _ in range(2):  # relaunch (graph replay) gives the same result
+        rep = grp.launch()
+        assert rep.kernels >= 1
+        for X1, X2, X3, r1, out, _ in host:
+            R = np.einsum("xay,asb->xsyb", X1.astype(np.complex128), X2.astype(np.complex128))
+            ref = np.einsum("xsyb,ytb->xst", R, X3.astype(np.complex128))
+            for got, want in ((r1, R), (out, ref)):
+                mx, fro = no.rel_errors(got.cpu().numpy(), want)
+                assert mx < 2e-6 and fro < 2e-6, (mx, fro)
+    grp.close()
+    if autotune:
+        assert (tmp_path / "tune.txt").exists()
+
+
+def test_all_tensor_core_batch_with_dependencies(ctx, torch_cuda):
+    """Every item on the tensor cores and two dependency levels: one
+    persistent launch resolves the dependencies in the kernel."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    rng = np.random.default_rng(32)
+    v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+    items, checks = [], []
+    for _ in range(5):
+        x, a, y, b, q = (int(val) for val in rng.choice([32, 48, 64, 96], 5))
+        X1 = _rand(rng, (x, a), np.complex64, 0.2)
+        X2 = _rand(rng, (a, y, b), np.complex64, 0.2)
+        X3 = _rand(rng, (y, b, q), np.complex64, 0.2)
+        g1, g2, g3 = (torch.from_numpy(val.copy()).cuda() for val in (X1, X2, X3))
+        r1 = torch.zeros((x, y, b), dtype=torch.complex64, device="cuda")
+        out = torch.zeros((x, q), dtype=torch.complex64, device="cuda")
+        i1 = len(items)
+        items.append((1.0, v(g1), "xa", v(g2), "ayb", 0.0, v(r1), "xyb", -1))
+        items.append((0.5j, v(r1), "xyb", v(g3), "ybq", 0.0, v(out), "xq", i1))
+        checks.append((X1, X2, X3, r1, out, (g1, g2, g3)))
+    grp = t1m.Group(items, ctx=ctx, graph=True)
+    rep = grp.launch()
+    assert rep.kernels == 1
+    for X1, X2, X3, r1, out, _ in checks:
+        R = np.einsum("xa,ayb->xyb", X1.astype(np.complex128), X2.astype(np.complex128))
+        ref = 0.5j * np.einsum("xyb,ybq->xq", R, X3.astype(np.complex128))
+        for got, want in ((r1, R), (out, ref)):
+            mx, fro = no.rel_errors(got.cpu().numpy(), want)
+            assert mx < 2e-6 and fro < 2e-6, (mx, fro)
+    grp.close()
+
+
+def test_group_equals_one_call_at_a_time(ctx, torch_cuda):
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    rng = np.random.default_rng(33)
+    items, host = _sweep_items(torch, t1m, rng, 4, [16, 32, 64], [2, 4])
+    grp = t1m.Group(items, ctx=ctx, graph=True)
+    grp.launch()
+    grouped = [(r1.clone(), out.clone()) for _, _, _, r1, out, _ in host]
+    for (alpha, a, la, b, lb, beta, c, lc, _dep) in items:
+        t1m.contract_scaled(alpha, a, la, b, lb, beta, c, lc, ctx=ctx)
+    torch.cuda.synchronize()
+    # Both may pick different kernels per item (the group's skinny plain tile
+    # vs the per-call choice), so both are held to the FP64 oracle; the plain
+    # form's sequential FP32 error grows like u*sqrt(2K).
+    for (g_r1, g_out), (X1, X2, X3, r1, out, _) in zip(grouped, host):
+        R = np.einsum("xay,asb->xsyb", X1.astype(np.complex128), X2.astype(np.complex128))
+        ref = np.einsum("xsyb,ytb->xst", R, X3.astype(np.complex128))
+        k2 = X3.shape[0] * X3.shape[2]
+        tol = max(2e-6, 4 * 2.0 ** -24 * np.sqrt(2.0 * k2))
+        for got in (g_out, out):
+            mx, _ = no.rel_errors(got.cpu().numpy(), ref)
+            assert mx < tol, (mx, tol)
+        for got in (g_r1, r1):
+            mx, _ = no.rel_errors(got.cpu().numpy(), R)
+            assert mx < 2e-6, mx
+    grp.close()
+
+
+def test_group_rejects_forward_dependency_and_host_data(ctx, torch_cuda):
+    import t1m_gb300 as t1m
+    A = np.ones((2, 3), np.complex64)
+    B = np.ones((3, 2), np.complex64)
+    Cm = np.zeros((2, 2), np.complex64)
+    v = t1m.tensor.from_array
+    with pytest.raises(t1m.T1MError):
+        t1m.Group([(1.0, v(A), "ab", v(B), "bc", 0.0, v(Cm), "ac", -1)], ctx=ctx)
+    torch = torch_cuda
+    g = [torch.from_numpy(x).cuda() for x in (A, B, Cm)]
+    w = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+    with pytest.raises(t1m.T1MError):
+        t1m.Group([(1.0, w(g[0]), "ab", w(g[1]), "bc", 0.0, w(g[2]), "ac", 1)], ctx=ctx)
