@@ -61,6 +61,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -98,6 +99,10 @@ constexpr int kBarrierBytes = 256;
 constexpr int kSmemBytes = 1024 + kRaw * kRawBytes + kStages * kOpBytes + kBarrierBytes;
 constexpr uint32_t kIdesc = ptx::idesc_f32acc(2u /*TF32*/, 128, kTileN);
 
+constexpr uint32_t kRegsLaunch = 168;   // 65536 / 384, rounded down to a multiple of 8
+constexpr uint32_t kRegsControl = 96;   // warpgroup 0: MMA issue + loaders
+constexpr uint32_t kRegsConvert = 200;  // warpgroups 1-2: converters
+static_assert(4 * kRegsControl + 8 * kRegsConvert <= 12 * kRegsLaunch, "register split");
 static_assert(kAStageCol + 64 * kStages <= kTmemCols, "TMEM budget");
 static_assert(kSmemBytes <= 227 * 1024, "shared memory budget");
 static_assert(kRawABytes % 1024 == 0 && kRawBBytes % 1024 == 0, "TMA swizzle alignment");
@@ -281,6 +286,15 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
   __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot_ptr;
+
+  // Register budget: the MMA/loader warpgroup needs few registers, the two
+  // converter warpgroups hold 64 accumulator floats each plus the stage data.
+  // 4 warps x 96 + 8 warps x 200 registers (x 32 lanes) = 63,488 <= the
+  // 384 x 168 = 64,512 the block is launched with.
+  if (warp < 4)
+    ptx::regs_dec<kRegsControl>();
+  else
+    ptx::regs_inc<kRegsConvert>();
 
   if (warp == 0) {
     // ---------------------------------------------------------- MMA issue ---
@@ -466,80 +480,80 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
     };
 
     bool ok = true;
-    int64_t raw_cnt = 0, op_cnt = 0, chunk_cnt = 0, tile_cnt = 0;
-    for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++tile_cnt) {
-      const TileRef tr = locate(&single, group, nprob, t);
-      const TcProblem* p = tr.p;
-      const GemmArgs& g = p->g;
-      const int amode = p->amode, bmode = p->bmode;
-      const bool conjA = g.flags & kFlagConjA;
-      const bool conjB = g.flags & kFlagConjB;
-      const bool row_ok = (tr.m0 + ci) < g.M;
+    // Ring positions (index and phase parity) carried from tile to tile.
+    uint32_t rr = 0, rph = 0, st = 0, sph = 0;
+    int64_t chunk_cnt = 0, tile_cnt = 0;
 
-      // Shared-memory offsets of this thread's raw reads and operand writes.
-      uint32_t aoff[8];
+    // One tile's stage loop for one (A layout, B layout) pair; the layout
+    // decisions are compile-time inside, taken once per tile outside.
+    //   A layouts: 0 = [k][m] rows of 512 B, 1 = four [16 k][16 m] blocks,
+    //              2 = [m][k] 128 B swizzled;  B: 0 = [n][k] swizzled, 1 = [k][n].
+    auto run_stages = [&](auto alay, auto blay, const TileRef& tr, bool conjA, bool conjB,
+                          bool row_ok, int64_t chunk_base) -> bool {
+      constexpr int AL = decltype(alay)::value;
+      constexpr int BL = decltype(blay)::value;
+      // Offsets of this thread's raw reads and operand writes.  Where they are
+      // affine in the unrolled index (base + j*stride) only the base is kept,
+      // so the strides become immediate offsets of the shared-memory accesses.
+      uint32_t aoff_sw[4];  // [m][k] swizzled A: four 16-byte chunks
+      uint32_t abase;
+      if constexpr (AL == 2) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        if (amode == kAKM)
-          aoff[j] = swz128(ci, 8 * wg + 2 * (j >> 1));
-        else if (amode == kAMK16)
-          aoff[j] = static_cast<uint32_t>((ci >> 4) * 2048 + (8 * wg + j) * 128 + (ci & 15) * 8);
-        else
-          aoff[j] = static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8);
+        for (int j = 0; j < 4; ++j) aoff_sw[j] = swz128(ci, 8 * wg + 2 * j);
+        abase = 0;
+      } else if constexpr (AL == 1) {
+        abase = static_cast<uint32_t>((ci >> 4) * 2048 + (8 * wg) * 128 + (ci & 15) * 8);
+      } else {
+        abase = static_cast<uint32_t>((8 * wg) * 512 + ci * 8);
       }
-      uint32_t bsrc[4], boff[4][2];
+      constexpr uint32_t kAStep = AL == 1 ? 128u : 512u;
+      // B: piece j of this thread is piece 0 plus 4096 j bytes in both the raw
+      // tile and (for [n][k]) the swizzled operand tile.
+      const uint32_t bsrc0 = BL == 1 ? static_cast<uint32_t>((pt >> 6) * 1024 + 2 * (pt & 63) * 8)
+                                     : swz128(pt >> 3, 2 * (pt & 7));
+      uint32_t boff_kn[4][2];
+      if constexpr (BL == 1) {
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const int id = pt + 256 * j;
-        if (bmode == kBKN) {
-          const int k = id >> 6, n = 2 * (id & 63);
-          bsrc[j] = static_cast<uint32_t>(k * 1024 + n * 8);
-          boff[j][0] = swz128(n, k);
-          boff[j][1] = swz128(n + 1, k);
-        } else {
-          const int n = id >> 3, kp = id & 7;
-          bsrc[j] = swz128(n, 2 * kp);
-          boff[j][0] = bsrc[j];
-          boff[j][1] = 0;
+        for (int j = 0; j < 4; ++j) {
+          const int k = (pt >> 6) + 4 * j, n = 2 * (pt & 63);
+          boff_kn[j][0] = swz128(n, k);
+          boff_kn[j][1] = swz128(n + 1, k);
         }
       }
-#pragma unroll
-      for (int j = 0; j < 64; ++j) master[j] = 0.f;
-
-      const int64_t chunk_base = chunk_cnt;
-      for (int64_t s = 0; s < tr.ksteps; ++s, ++raw_cnt, ++op_cnt) {
-        const int r = static_cast<int>(raw_cnt % kRaw);
-        const uint32_t rph = static_cast<uint32_t>((raw_cnt / kRaw) & 1);
-        const int st = static_cast<int>(op_cnt % kStages);
-        const uint32_t ph = static_cast<uint32_t>((op_cnt / kStages) & 1);
-        if (!ptx::mbar_wait(raw_full(r), rph)) {
+      const int ksteps = static_cast<int>(tr.ksteps);
+      for (int s = 0; s < ksteps; ++s) {
+        if (!ptx::mbar_wait(raw_full(rr), rph)) {
           record_error(err_flag, kErrRawWait);
-          ok = false;
-          break;
+          return false;
         }
-        const uint32_t ra = raw_a(r), rb = raw_b(r);
+        const uint32_t ra = raw_a(rr), rb = raw_b(rr);
         float2 av[8];
-        if (amode == kAKM) {
+        if constexpr (AL == 2) {
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            const float4 v = lds128(ra + aoff[2 * j]);
+            const float4 v = lds128(ra + aoff_sw[j]);
             av[2 * j] = make_float2(v.x, v.y);
             av[2 * j + 1] = make_float2(v.z, v.w);
           }
         } else {
+          const uint32_t a0 = ra + abase;
 #pragma unroll
-          for (int j = 0; j < 8; ++j) av[j] = lds64(ra + aoff[j]);
+          for (int j = 0; j < 8; ++j) av[j] = lds64(a0 + kAStep * j);
         }
         float4 bv[4];
+        const uint32_t b0 = rb + bsrc0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
+        for (int j = 0; j < 4; ++j) bv[j] = lds128(b0 + 4096u * j);
         __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(raw_empty(r));
+        if (lane == 0) ptx::mbar_arrive(raw_empty(rr));
+        if (++rr == kRaw) {
+          rr = 0;
+          rph ^= 1u;
+        }
 
-        if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
+        if (!ptx::mbar_wait(empty_bar(st), sph ^ 1u)) {
           record_error(err_flag, kErrEmptyWait);
-          ok = false;
-          break;
+          return false;
         }
         ptx::tc_fence_after();
         // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
@@ -571,14 +585,15 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           }
           const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
           const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
-          if (bmode == kBKN) {
-            sts64(ob + boff[j][0], r0.hi, i0.hi);
-            sts64(ob + boff[j][1], r1.hi, i1.hi);
-            sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
-            sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
+          if constexpr (BL == 1) {
+            sts64(ob + boff_kn[j][0], r0.hi, i0.hi);
+            sts64(ob + boff_kn[j][1], r1.hi, i1.hi);
+            sts64(ob + kBHalfBytes + boff_kn[j][0], r0.lo, i0.lo);
+            sts64(ob + kBHalfBytes + boff_kn[j][1], r1.lo, i1.lo);
           } else {
-            sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
-            sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+            const uint32_t o = ob + bsrc0 + 4096u * j;
+            sts128(o, r0.hi, i0.hi, r1.hi, i1.hi);
+            sts128(o + kBHalfBytes, r0.lo, i0.lo, r1.lo, i1.lo);
           }
         }
         ptx::tmem_wait_st();
@@ -586,6 +601,10 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         ptx::tc_fence_before();
         __syncwarp();
         if (lane == 0) ptx::mbar_arrive(full_bar(st));
+        if (++st == kStages) {
+          st = 0;
+          sph ^= 1u;
+        }
 
         // Fold the previous chunk once the first stage of the next is queued.
         if ((s % kFold) == 0 && s >= kFold) {
@@ -593,8 +612,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           const int buf = static_cast<int>(c & 1);
           if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
             record_error(err_flag, kErrChunkWait);
-            ok = false;
-            break;
+            return false;
           }
           ptx::tc_fence_after();
           fold_from(buf ? kChunkCol1 : kChunkCol0);
@@ -602,6 +620,33 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           __syncwarp();
           if (lane == 0) ptx::mbar_arrive(chunk_empty(buf));
         }
+      }
+      return true;
+    };
+
+    for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++tile_cnt) {
+      const TileRef tr = locate(&single, group, nprob, t);
+      const TcProblem* p = tr.p;
+      const GemmArgs& g = p->g;
+      const int amode = p->amode, bmode = p->bmode;
+      const bool conjA = g.flags & kFlagConjA;
+      const bool conjB = g.flags & kFlagConjB;
+      const bool row_ok = (tr.m0 + ci) < g.M;
+#pragma unroll
+      for (int j = 0; j < 64; ++j) master[j] = 0.f;
+      const int64_t chunk_base = chunk_cnt;
+      using I0 = std::integral_constant<int, 0>;
+      using I1 = std::integral_constant<int, 1>;
+      using I2 = std::integral_constant<int, 2>;
+      const int alay = amode == kAKM ? 2 : (amode == kAMK16 ? 1 : 0);
+      const int blay = bmode == kBKN ? 1 : 0;
+      switch (alay * 2 + blay) {
+        case 0: ok = run_stages(I0{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 1: ok = run_stages(I0{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 2: ok = run_stages(I1{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 3: ok = run_stages(I1{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 4: ok = run_stages(I2{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        default: ok = run_stages(I2{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
       }
       if (!ok) break;
 
@@ -676,6 +721,404 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
   }
 }
 
+// --------------------------------------------- one tile per CTA variant ---
+// For a single contraction whose operands are a uniform 2-D view or gathered,
+// this non-persistent form (one output tile per CTA, operand modes as template
+// parameters) measured faster than the persistent kernel on GB300 (2.81 ms vs
+// 3.06-3.10 ms for complex64 4096^3), so single contractions use it when their
+// fetch modes allow; the persistent kernel serves grouped launches and the
+// per-16-row block TMA modes.
+enum : int { kTmaMK = 0, kTmaKM = 1, kGatherMK = 2 };
+enum : int { kTmaNK = 0, kTmaKN = 1, kGatherNK = 2 };
+
+struct TmaMaps {
+  CUtensorMap a;
+  CUtensorMap b;
+};
+
+template <int AMode, int BMode>
+__global__ void __launch_bounds__(kThreads, 1)
+tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
+  constexpr bool kTmaA = AMode != kGatherMK;
+  constexpr bool kTmaB = BMode != kGatherNK;
+  constexpr bool kGather = !kTmaA || !kTmaB;
+  // Arrivals per raw stage: one expect_tx arrive from the TMA thread, one
+  // cp.async completion arrive per gather thread.
+  constexpr uint32_t kRawArrivals = (kTmaA || kTmaB ? 1u : 0u) + (kGather ? kLoaders : 0u);
+  constexpr uint32_t kTmaBytes = (kTmaA ? kRawABytes : 0) + (kTmaB ? kRawBBytes : 0);
+
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  const uint32_t base = (ptx::smem_u32(smem_raw) + 1023u) & ~1023u;
+  uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
+  const uint32_t raw0 = base;                          // kRaw x (A 8 KB | B 16 KB)
+  const uint32_t op0 = raw0 + kRaw * kRawBytes;        // kStages x (B hi | B lo)
+  const uint32_t bars = op0 + kStages * kOpBytes;
+  auto raw_a = [&](int r) { return raw0 + r * kRawBytes; };
+  auto raw_b = [&](int r) { return raw0 + r * kRawBytes + kRawABytes; };
+  auto raw_full = [&](int r) { return bars + 8u * r; };
+  auto raw_empty = [&](int r) { return bars + 8u * (kRaw + r); };
+  auto full_bar = [&](int s) { return bars + 8u * (2 * kRaw + s); };
+  auto empty_bar = [&](int s) { return bars + 8u * (2 * kRaw + kStages + s); };
+  auto chunk_full = [&](int b) { return bars + 8u * (2 * kRaw + 2 * kStages + b); };
+  auto chunk_empty = [&](int b) { return bars + 8u * (2 * kRaw + 2 * kStages + 2 + b); };
+  const uint32_t acc_bar = bars + 8u * (2 * kRaw + 2 * kStages + 4);
+  const uint32_t tmem_slot = acc_bar + 8u;
+  volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(base_ptr + (tmem_slot - base));
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+
+  if (warp == 0) {
+    ptx::tmem_alloc(tmem_slot, kTmemCols);
+    ptx::tmem_relinquish();
+  }
+  if (tid == 32) {
+    for (int r = 0; r < kRaw; ++r) {
+      ptx::mbar_init(raw_full(r), kRawArrivals);
+      ptx::mbar_init(raw_empty(r), kConverters / 32);
+    }
+    for (int s = 0; s < kStages; ++s) {
+      ptx::mbar_init(full_bar(s), kConverters / 32);
+      ptx::mbar_init(empty_bar(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(chunk_full(b), 1);
+      ptx::mbar_init(chunk_empty(b), kConverters / 32);
+    }
+    ptx::mbar_init(acc_bar, 1);
+    ptx::fence_mbar_init();
+  }
+  if (tid == 64) {
+    if (kTmaA) ptx::tma_prefetch_desc(&maps.a);
+    if (kTmaB) ptx::tma_prefetch_desc(&maps.b);
+  }
+  ptx::tc_fence_before();
+  __syncthreads();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot_ptr;
+
+  const int64_t M = args.M, N = args.N;
+  // Split-K: this CTA row covers K range [kb, K) (kb a multiple of kStepK).
+  const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
+  const int64_t K = min(args.K, kb + args.k_per_split);
+  const int64_t tiles_m = (M + kTileMc - 1) / kTileMc;
+  const int64_t tiles_n = (N + kTileN - 1) / kTileN;
+  // Groups of 16 M-tiles sweep N so CTAs running together share B in L2.
+  constexpr int64_t G = 16;
+  const int64_t t = blockIdx.x;
+  const int64_t group = t / (G * tiles_n);
+  const int64_t first_m = group * G;
+  const int64_t gsize = min(G, tiles_m - first_m);
+  const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
+  const int64_t tn = (t % (G * tiles_n)) / gsize;
+  const int64_t m0 = tm * kTileMc, n0 = tn * kTileN;
+  const int64_t ksteps = (K - kb + kStepK - 1) / kStepK;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------- MMA issue ---
+    if (lane == 0) {
+      for (int64_t s = 0; s < ksteps; ++s) {
+        const int st = static_cast<int>(s % kStages);
+        const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
+        const int64_t c = s / kFold;
+        const int buf = static_cast<int>(c & 1);
+        const bool chunk_start = (s % kFold) == 0;
+        if (chunk_start && c >= 2 &&
+            !ptx::mbar_wait(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
+          record_error(err_flag, kErrChunkWait);
+          break;
+        }
+        if (!ptx::mbar_wait(full_bar(st), ph)) {
+          record_error(err_flag, kErrFullWait);
+          break;
+        }
+        ptx::tc_fence_after();
+        const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
+        const uint32_t d_corr = tmem + kCorrCol;
+        const uint32_t a_hi = tmem + kAStageCol + 64u * st;
+        const uint32_t a_lo = a_hi + 32u;
+        const uint32_t b_hi = op0 + st * kOpBytes;
+        const uint32_t b_lo = b_hi + kBHalfBytes;
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
+          const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
+          ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
+          ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
+          ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
+        }
+        ptx::mma_commit(empty_bar(st));
+        if ((s % kFold) == kFold - 1 || s == ksteps - 1) ptx::mma_commit(chunk_full(buf));
+      }
+      // Signal the epilogue (also after an abort, so nobody waits forever),
+      // then make sure no MMA is still writing TMEM before it is freed.
+      ptx::mma_commit(acc_bar);
+      if (!ptx::mbar_wait(acc_bar, 0)) record_error(err_flag, kErrAccWait);
+    }
+    __syncwarp();
+  } else if (tid < kConvBase) {
+    // ------------------------------------------------------------ loaders ---
+    const int lt = tid - kLoaderBase;  // 0..95
+    const float2* __restrict__ A = static_cast<const float2*>(args.A);
+    const float2* __restrict__ B = static_cast<const float2*>(args.B);
+    // Gather work of this thread: fixed rows / columns, K walked per stage.
+    for (int64_t s = 0; s < ksteps; ++s) {
+      const int r = static_cast<int>(s % kRaw);
+      const uint32_t ph = static_cast<uint32_t>((s / kRaw) & 1);
+      const int64_t k0 = kb + s * kStepK;
+      if (kGather || lt == 0) {
+        if (!ptx::mbar_wait(raw_empty(r), ph ^ 1u)) {
+          record_error(err_flag, kErrRawWait);
+          break;
+        }
+      }
+      if ((kTmaA || kTmaB) && lt == 0) {
+        ptx::mbar_arrive_expect_tx(raw_full(r), kTmaBytes);
+        if (AMode == kTmaMK)
+          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * m0), static_cast<int>(k0), raw_full(r));
+        if (AMode == kTmaKM)
+          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * k0), static_cast<int>(m0), raw_full(r));
+        if (BMode == kTmaNK)
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * k0), static_cast<int>(n0), raw_full(r));
+        if (BMode == kTmaKN)
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * n0), static_cast<int>(k0), raw_full(r));
+      }
+      if (kGather) {
+        if (AMode == kGatherMK) {
+          // [k][m]: consecutive threads walk m (coalesced where M is unit stride).
+          for (int e = lt; e < kTileMc * kStepK; e += kLoaders) {
+            const int m = e % kTileMc, k = e / kTileMc;
+            const bool ok = (m0 + m < M) && (k0 + k < K);
+            const float2* src = ok ? A + offs(args.rsA, args.uA_m, m0 + m) + offs(args.csA, args.uA_k, k0 + k) : A;
+            ptx::cp_async_8(raw_a(r) + static_cast<uint32_t>(k * 512 + m * 8), src, ok ? 8u : 0u);
+          }
+        }
+        if (BMode == kGatherNK) {
+          // [n][k] swizzled: consecutive threads walk k.
+          for (int e = lt; e < kTileN * kStepK; e += kLoaders) {
+            const int k = e % kStepK, n = e / kStepK;
+            const bool ok = (n0 + n < N) && (k0 + k < K);
+            const float2* src = ok ? B + offs(args.rsB, args.uB_k, k0 + k) + offs(args.csB, args.uB_n, n0 + n) : B;
+            ptx::cp_async_8(raw_b(r) + swz128(n, k), src, ok ? 8u : 0u);
+          }
+        }
+        ptx::cp_async_arrive_noinc(raw_full(r));
+      }
+    }
+  } else {
+    // -------------------------------------------- converters, fold, epilogue ---
+    const int pt = tid - kConvBase;
+    const int wg = pt >> 7;          // which half of the K-step (A) / of N (B, C)
+    const int q = (pt >> 5) & 3;     // TMEM lane quarter of this warp
+    const int rho = 32 * q + lane;   // real row = TMEM lane
+    const int ci = rho >> 1;         // complex row in the tile
+    const int part = rho & 1;        // 0: real row "re", 1: "im"
+    const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
+    const bool conjA = args.flags & kFlagConjA;
+    const bool conjB = args.flags & kFlagConjB;
+    const bool row_ok = (m0 + ci) < M;
+
+    float master[64];
+#pragma unroll
+    for (int j = 0; j < 64; ++j) master[j] = 0.f;
+
+    // Fold chunk accumulator at column `col` into the FP32 master registers
+    // (round-to-nearest adds): this thread's lane, 64 columns.
+    auto fold_from = [&](uint32_t col) {
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) {
+        uint32_t r[16];
+        ptx::tmem_ld16(tmem + lane_base + col + 64u * wg + 16u * cc, r);
+        ptx::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) master[16 * cc + j] += __uint_as_float(r[j]);
+      }
+    };
+
+    // Loop-invariant shared-memory offsets of this thread's raw reads and
+    // operand writes.
+    uint32_t aoff[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      aoff[j] = (AMode == kTmaKM) ? swz128(ci, 8 * wg + 2 * (j >> 1))
+                                  : static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8);
+    uint32_t bsrc[4], boff[4][2];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int id = pt + 256 * j;
+      if (BMode == kTmaKN) {
+        const int k = id >> 6, n = 2 * (id & 63);
+        bsrc[j] = static_cast<uint32_t>(k * 1024 + n * 8);
+        boff[j][0] = swz128(n, k);
+        boff[j][1] = swz128(n + 1, k);
+      } else {
+        const int n = id >> 3, kp = id & 7;
+        bsrc[j] = swz128(n, 2 * kp);
+        boff[j][0] = bsrc[j];
+        boff[j][1] = 0;
+      }
+    }
+
+    bool ok = true;
+    int r = 0, st = 0;
+    uint32_t rph = 0, ph = 0;
+    for (int64_t s = 0; s < ksteps; ++s) {
+      if (!ptx::mbar_wait(raw_full(r), rph)) {
+        record_error(err_flag, kErrRawWait);
+        ok = false;
+        break;
+      }
+      // A: eight complex k (this half of the step) of complex row ci.
+      const uint32_t ra = raw_a(r), rb = raw_b(r);
+      float2 av[8];
+      if (AMode == kTmaKM) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float4 v = lds128(ra + aoff[2 * j]);
+          av[2 * j] = make_float2(v.x, v.y);
+          av[2 * j + 1] = make_float2(v.z, v.w);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) av[j] = lds64(ra + aoff[j]);
+      }
+      // B: four 16-byte pieces (two complex each) of the raw tile.
+      float4 bv[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(raw_empty(r));
+
+      if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
+        record_error(err_flag, kErrEmptyWait);
+        ok = false;
+        break;
+      }
+      ptx::tc_fence_after();
+      // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
+      uint32_t hi[16], lo[16];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        float2 v = av[j];
+        if (conjA) v.y = -v.y;
+        if (!row_ok) v = make_float2(0.f, 0.f);
+        const float x0 = part ? v.y : v.x;
+        const float x1 = part ? v.x : -v.y;
+        const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
+        hi[2 * j] = s0.hi;
+        lo[2 * j] = s0.lo;
+        hi[2 * j + 1] = s1.hi;
+        lo[2 * j + 1] = s1.lo;
+      }
+      const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 16u * wg;
+      ptx::tmem_st16(a_col, hi);
+      ptx::tmem_st16(a_col + 32u, lo);
+      // B -> shared memory (swizzled K-major hi and lo tiles).
+      const uint32_t ob = op0 + st * kOpBytes;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float4 v = bv[j];
+        if (conjB) {
+          v.y = -v.y;
+          v.w = -v.w;
+        }
+        const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
+        const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
+        if (BMode == kTmaKN) {
+          sts64(ob + boff[j][0], r0.hi, i0.hi);
+          sts64(ob + boff[j][1], r1.hi, i1.hi);
+          sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
+          sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
+        } else {
+          sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
+          sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+        }
+      }
+      ptx::tmem_wait_st();
+      ptx::fence_proxy_async_smem();
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive(full_bar(st));
+
+      // Fold the previous chunk once the first stage of the next is queued.
+      if ((s % kFold) == 0 && s >= kFold) {
+        const int64_t c = s / kFold - 1;
+        const int buf = static_cast<int>(c & 1);
+        if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
+          record_error(err_flag, kErrChunkWait);
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        fold_from(buf ? kChunkCol1 : kChunkCol0);
+        ptx::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(chunk_empty(buf));
+      }
+      if (++r == kRaw) {
+        r = 0;
+        rph ^= 1u;
+      }
+      if (++st == kStages) {
+        st = 0;
+        ph ^= 1u;
+      }
+    }
+
+    // ---------------------------------------------------------- epilogue ---
+    if (!ptx::mbar_wait(acc_bar, 0)) {
+      record_error(err_flag, kErrAccWait);
+      ok = false;
+    }
+    ptx::tc_fence_after();
+    if (ok) {
+      // The last chunk was never folded in the loop; then add the corrections.
+      const int64_t c_last = (ksteps - 1) / kFold;
+      fold_from((c_last & 1) ? kChunkCol1 : kChunkCol0);
+      fold_from(kCorrCol);
+      const bool accumulate = args.flags & kFlagAccumulate;
+      const bool beta_zero = args.flags & kFlagBetaZero;
+      const float ar = (float)args.alpha[0], ai = (float)args.alpha[1];
+      const float br = (float)args.beta[0], bi = (float)args.beta[1];
+      float2* __restrict__ Cp =
+          static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
+      const int64_t rowC = row_ok ? offs(args.rsC, args.uC_m, m0 + ci) : 0;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const float v0 = master[2 * j], v1 = master[2 * j + 1];
+        const float send = part ? v0 : v1;
+        const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
+        const int col = wg * 64 + 2 * j + part;
+        const float re = part ? recv : v0;
+        const float im = part ? v1 : recv;
+        const int64_t n = n0 + col;
+        if (row_ok && n < N) {
+          float2* p = Cp + rowC + offs(args.csC, args.uC_n, n);
+          const float tr = ar * re - ai * im;
+          const float ti = ar * im + ai * re;
+          if (accumulate) {
+            const float2 o = *p;
+            *p = make_float2(o.x + tr, o.y + ti);
+          } else if (beta_zero) {
+            *p = make_float2(tr, ti);
+          } else {
+            const float2 o = *p;
+            *p = make_float2(tr + (br * o.x - bi * o.y), ti + (br * o.y + bi * o.x));
+          }
+        }
+      }
+    }
+  }
+
+  ptx::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc(tmem, kTmemCols);
+  }
+}
+
+
 // ------------------------------------------------------------------ host ---
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                    const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
@@ -730,6 +1173,30 @@ bool unit_blocks16(const std::vector<int64_t>& v, int64_t n) {
   return true;
 }
 
+template <int AMode, int BMode>
+cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
+                         int* err_flag, dim3 tiles) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(tc3xtf32_contract<AMode, BMode>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  tc3xtf32_contract<AMode, BMode><<<tiles, kThreads, kSmemBytes, stream>>>(args, maps, err_flag);
+  return cudaGetLastError();
+}
+
+template <int AMode>
+cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
+                     int* err_flag, dim3 tiles) {
+  switch (bmode) {
+    case kTmaNK: return launch_modes<AMode, kTmaNK>(args, maps, stream, err_flag, tiles);
+    case kTmaKN: return launch_modes<AMode, kTmaKN>(args, maps, stream, err_flag, tiles);
+    default: return launch_modes<AMode, kGatherNK>(args, maps, stream, err_flag, tiles);
+  }
+}
+
 std::mutex g_attr_mutex;
 bool g_attr_set = false;
 
@@ -763,11 +1230,14 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
            make_map(&p->map_a, g.A, g.K, g.M, plan.uA_m, 2 * kStepK, kTileMc, true))
     p->amode = kAKM;
   else if (plan.uA_k >= 0 && unit_blocks16(plan.rsA, g.M) &&
-           make_map(&p->map_a, g.A, plan.spanA, g.K, plan.uA_k, 32, kStepK, false))
+           make_map(&p->map_a, g.A, plan.spanA, g.K, plan.uA_k, 32, kStepK, false)) {
     p->amode = kAMK16;
-  else if (plan.uA_m >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.csA, g.K) &&
-           make_map(&p->map_a, g.A, plan.spanA, g.M, plan.uA_m, 2 * kStepK, kTileMc, true))
+    p->block_maps |= 1;
+  } else if (plan.uA_m >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.csA, g.K) &&
+             make_map(&p->map_a, g.A, plan.spanA, g.M, plan.uA_m, 2 * kStepK, kTileMc, true)) {
     p->amode = kAKM;
+    p->block_maps |= 1;
+  }
   // B: TMA over a uniform 2-D view or per unit-stride 16-element K block, or gather.
   p->bmode = kBGather;
   if (plan.uB_k == 1 && plan.uB_n >= 0 &&
@@ -777,8 +1247,10 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
            make_map(&p->map_b, g.B, g.N, g.K, plan.uB_k, 2 * kTileN, kStepK, false))
     p->bmode = kBKN;
   else if (plan.uB_n >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.rsB, g.K) &&
-           make_map(&p->map_b, g.B, plan.spanB, g.N, plan.uB_n, 2 * kStepK, kTileN, true))
+           make_map(&p->map_b, g.B, plan.spanB, g.N, plan.uB_n, 2 * kStepK, kTileN, true)) {
     p->bmode = kBNK;
+    p->block_maps |= 2;
+  }
   return true;
 }
 
@@ -834,8 +1306,24 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   p.dep = -1;
-  const cudaError_t e =
-      tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
+  cudaError_t e;
+  if (p.block_maps == 0 && p.amode != kAMK16) {
+    // Uniform or gathered operands: the one-tile-per-CTA form.
+    TmaMaps maps;
+    maps.a = p.map_a;
+    maps.b = p.map_b;
+    const dim3 grid(static_cast<unsigned>(int64_t(p.tiles_m) * p.tiles_n),
+                    static_cast<unsigned>(splits));
+    const int am = p.amode == kAMK ? kTmaMK : (p.amode == kAKM ? kTmaKM : kGatherMK);
+    const int bm = p.bmode == kBNK ? kTmaNK : (p.bmode == kBKN ? kTmaKN : kGatherNK);
+    switch (am) {
+      case kTmaMK: e = launch_b<kTmaMK>(bm, args, maps, stream, err_flag, grid); break;
+      case kTmaKM: e = launch_b<kTmaKM>(bm, args, maps, stream, err_flag, grid); break;
+      default: e = launch_b<kGatherMK>(bm, args, maps, stream, err_flag, grid); break;
+    }
+  } else {
+    e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
+  }
   if (e == cudaSuccess) *kernels = 1;
   return e;
 }

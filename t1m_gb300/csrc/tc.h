@@ -23,7 +23,7 @@ namespace gb300 {
 enum : int32_t { kAGather = 0, kAMK = 1, kAMK16 = 2, kAKM = 3 };
 enum : int32_t { kBGather = 0, kBNK = 1, kBKN = 2 };
 
-struct alignas(64) TcProblem {
+struct TcProblem {
   CUtensorMap map_a;
   CUtensorMap map_b;
   GemmArgs g;
@@ -34,7 +34,9 @@ struct alignas(64) TcProblem {
   // been written.
   int32_t dep;
   int32_t dep_tiles;
-  int32_t reserved;
+  // Bit 0: A's map is a per-16-element block map (coordinates from the
+  // scatter vector); bit 1: the same for B.
+  int32_t block_maps;
   int64_t tile_begin;  // first tile of this problem in the launch's tile list
 };
 
