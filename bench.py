@@ -380,6 +380,238 @@ def run_gpu(args) -> None:
         dist.destroy_process_group()
 
 
+# --------------------------------------------------------- other workloads ---
+def _events_ms(torch, fn, steps, warmup):
+    """Mean ms of fn() over `steps`, CUDA events on torch's current stream
+    (callers run their context on that stream)."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(steps):
+        fn()
+    e.record()
+    e.synchronize()
+    return s.elapsed_time(e) / steps
+
+
+def _sampled_err(la, lb, lc, dims, ga, gb, gc, alpha=1.0, beta=0.0, gc0=None, samples=1024):
+    """Normwise errors at sampled C entries vs FP64 dot products (host numpy)."""
+    import numpy as np
+    da, db, dc = dims
+    cm = lambda d: [int(np.prod(d[:i])) for i in range(len(d))]  # noqa: E731 col-major
+    bd = _bundles(la, lb, lc)
+    scat = [_scatter(bd[k], d, cm(d)) for k, d in (("AX", da), ("AY", da), ("BX", db),
+                                                   ("BY", db), ("CX", dc), ("CY", dc))]
+    fa, fb, fc = ga.cpu().numpy(), gb.cpu().numpy(), gc.cpu().numpy()
+    rng = np.random.default_rng(3)
+    rows = rng.integers(0, len(scat[0]), samples)
+    cols = rng.integers(0, len(scat[3]), samples)
+    ab = np.einsum("sk,sk->s", fa[scat[0][rows][:, None] + scat[1][None, :]].astype(np.complex128),
+                   fb[scat[2][None, :] + scat[3][cols][:, None]].astype(np.complex128))
+    off = scat[4][rows] + scat[5][cols]
+    ref = alpha * ab
+    if gc0 is not None and beta != 0:
+        ref = ref + beta * gc0.cpu().numpy()[off].astype(np.complex128)
+    d = np.abs(fc[off].astype(np.complex128) - ref)
+    return float(d.max() / np.abs(ref).max()), float(np.linalg.norm(d) / np.linalg.norm(ref))
+
+
+def _bundles(la, lb, lc):
+    sa, sb = set(la), set(lb)
+    con, fa, fb = sorted(sa & sb), sorted(sa - sb), sorted(sb - sa)
+    return {"AX": [la.find(c) for c in fa], "AY": [la.find(c) for c in con],
+            "BX": [lb.find(c) for c in con], "BY": [lb.find(c) for c in fb],
+            "CX": [lc.find(c) for c in fa], "CY": [lc.find(c) for c in fb]}
+
+
+def _scatter(idx, dims, strides):
+    import numpy as np
+    out = np.zeros(1, dtype=np.int64)
+    for i in reversed(idx):
+        out = (out[:, None] + np.arange(dims[i], dtype=np.int64)[None, :] * strides[i]).reshape(-1)
+    return out
+
+
+def workload_config2(args):
+    """Plain GPU drop-in: abcd,efcd->abef (48^4) and abcd,dbea->ec, c64/c128,
+    col/row-major, alpha = 1+0.5i, beta = 0.25, every method."""
+    import torch
+    import t1m_gb300 as t1m
+    ctx = t1m.Context()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    dev = torch.device("cuda")
+    cases = []
+    shapes = [("abcd", "efcd", "abef", dict(a=48, b=48, c=48, d=48, e=48, f=48)),
+              ("abcd", "dbea", "ec", dict(a=24, b=32, c=96, d=48, e=64))]
+    for la, lb, lc, ext in shapes:
+        dims = [[ext[ch] for ch in s] for s in (la, lb, lc)]
+        for dt in (torch.complex64, torch.complex128):
+            g = torch.Generator(device=dev)
+            g.manual_seed(7)
+            rdt = torch.float32 if dt == torch.complex64 else torch.float64
+            mk = lambda n: torch.complex(torch.rand(n, device=dev, generator=g, dtype=rdt) * 2 - 1,  # noqa: E731
+                                         torch.rand(n, device=dev, generator=g, dtype=rdt) * 2 - 1)
+            ga, gb = mk(int(np.prod(dims[0]))), mk(int(np.prod(dims[1])))
+            gc0 = mk(int(np.prod(dims[2])))
+            methods = ["plain", "tc_3xtf32"] if dt == torch.complex64 else ["plain", "dmma"]
+            for layout in ("col", "row"):
+                L = t1m.col_major if layout == "col" else t1m.row_major
+                for m in methods:
+                    ctx.set_method(m)
+                    gc = gc0.clone()
+                    ta, tb, tc = (t1m.tensor(d, x, L) for d, x in zip(dims, (ga, gb, gc)))
+                    rep = t1m.contract_raw(1 + 0.5j, ta, la, tb, lb, 0.25, tc, lc, 0, ctx)
+                    if layout == "col":
+                        err = _sampled_err(la, lb, lc, dims, ga, gb, gc, 1 + 0.5j, 0.25, gc0)
+                    else:
+                        err = (None, None)
+                    ms = _events_ms(torch, lambda: t1m.contract_raw(
+                        1 + 0.5j, ta, la, tb, lb, 0.25, tc, lc, t1m.FLAG_NO_TIMING, ctx),
+                        args.steps, args.warmup)
+                    cases.append({"labels": f"{la},{lb}->{lc}", "dtype": str(dt).split(".")[1],
+                                  "layout": layout, "method": m, "split_k": rep.split_k,
+                                  "ms": ms, "tflops": rep.flops / ms / 1e9,
+                                  "rel_err_max": err[0], "rel_err_fro": err[1]})
+    ctx.close()
+    print(json.dumps({"workload": "config2 plain GPU drop-in", "cases": cases}), flush=True)
+
+
+def workload_logmag(args):
+    """Precision form, input set 2: |z| log-uniform over [1e-3, 1e3], uniform
+    phase, complex64 ijkl,klmn->ijmn extents 64; every method's error."""
+    import torch
+    import t1m_gb300 as t1m
+    ctx = t1m.Context()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev)
+    g.manual_seed(11)
+
+    def mk(n):
+        mag = torch.pow(10.0, torch.rand(n, device=dev, generator=g) * 6 - 3)
+        ph = torch.rand(n, device=dev, generator=g) * 2 * np.pi
+        return torch.polar(mag, ph)
+
+    ga, gb = mk(M * K), mk(K * N)
+    gc = torch.zeros(M * N, dtype=torch.complex64, device=dev)
+    dims = [[EXT] * 4] * 3
+    ta, tb, tc = (t1m.tensor(d, x) for d, x in zip(dims, (ga, gb, gc)))
+    out = []
+    for m in ("plain", "tc_3xtf32"):
+        ctx.set_method(m)
+        rep = t1m.contract_raw(1.0, ta, LA, tb, LB, 0.0, tc, LC, 0, ctx)
+        err = _sampled_err(LA, LB, LC, dims, ga, gb, gc)
+        out.append({"method": m, "ms": rep.kernel_ms, "tflops": FLOPS / rep.kernel_ms / 1e9,
+                    "rel_err_max": err[0], "rel_err_fro": err[1]})
+    ctx.close()
+    print(json.dumps({"workload": "config3 set 2 (log-uniform magnitudes)", "cases": out}),
+          flush=True)
+
+
+def workload_batch(args):
+    """Batching form: 1024 updates xay,asb->xsyb then xsyb,ytb->xst with
+    x, y, a, b ~ U{16..256 step 16}, s, t ~ U{2, 4}, components N(0, 1/sqrt(bond));
+    one grouped batch under a CUDA graph vs the same contractions one call at a time."""
+    import torch
+    import t1m_gb300 as t1m
+    n_items = args.items
+    ctx = t1m.Context()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    dev = torch.device("cuda")
+    rng = np.random.default_rng(2024)
+    bonds = np.arange(16, 257, 16)
+    items, flops, keep = [], 0.0, []
+    v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+    g = torch.Generator(device=dev)
+    g.manual_seed(5)
+    for _ in range(n_items):
+        x, y, a, b = (int(w) for w in rng.choice(bonds, 4))
+        s, t = (int(w) for w in rng.choice([2, 4], 2))
+
+        def mk(shape, bond):
+            sc = 1.0 / np.sqrt(np.sqrt(bond))
+            return torch.complex(torch.randn(shape, device=dev, generator=g) * sc,
+                                 torch.randn(shape, device=dev, generator=g) * sc)
+
+        X1, X2, X3 = mk((x, a, y), a), mk((a, s, b), a), mk((y, t, b), b)
+        R = torch.empty((x, s, y, b), dtype=torch.complex64, device=dev)
+        O = torch.empty((x, s, t), dtype=torch.complex64, device=dev)
+        i1 = len(items)
+        items.append((1.0, v(X1), "xay", v(X2), "asb", 0.0, v(R), "xsyb", -1))
+        items.append((1.0, v(R), "xsyb", v(X3), "ytb", 0.0, v(O), "xst", i1))
+        keep.append((X1, X2, X3, R, O))
+        flops += 8.0 * x * y * s * b * a + 8.0 * x * s * t * y * b
+    grp = t1m.Group(items, ctx=ctx, graph=True, autotune=True)
+    grouped_ms = _events_ms(torch, lambda: grp.launch(timed=False), args.steps, args.warmup)
+    # Sampled check of a few items against FP64.
+    errs = []
+    for X1, X2, X3, R, O in keep[:4]:
+        Rr = torch.einsum("xay,asb->xsyb", X1.to(torch.complex128), X2.to(torch.complex128))
+        Or = torch.einsum("xsyb,ytb->xst", Rr, X3.to(torch.complex128))
+        errs.append(float((O.to(torch.complex128) - Or).abs().max() / Or.abs().max()))
+
+    def one_by_one():
+        for (alpha, a_, la, b_, lb, beta, c_, lc, _d) in items:
+            t1m.contract_raw(alpha, a_, la, b_, lb, beta, c_, lc, t1m.FLAG_NO_TIMING, ctx)
+
+    single_ms = _events_ms(torch, one_by_one, max(1, args.steps // 2), 1)
+    grp.close()
+    ctx.close()
+    print(json.dumps({"workload": f"config4 batch of {n_items} sweep updates (2 contractions each)",
+                      "flops_per_batch": flops, "grouped_graph_ms": grouped_ms,
+                      "grouped_tflops": flops / grouped_ms / 1e9, "one_call_at_a_time_ms": single_ms,
+                      "one_call_tflops": flops / single_ms / 1e9,
+                      "speedup_grouped": single_ms / grouped_ms, "rel_err_max_sampled": max(errs)}),
+          flush=True)
+
+
+def workload_vjp(args):
+    """Differentiation form: abcd,ebfd->aecf extents 32 (complex64, tensor
+    cores), forward + adjoint (dA, dB) vs FP64, and the ring chain."""
+    import torch
+    import t1m_gb300 as t1m
+    from t1m_gb300.chain import ContractionChain
+    ctx = t1m.Context()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev)
+    g.manual_seed(9)
+    mk = lambda *s: torch.complex(torch.rand(s, device=dev, generator=g) * 2 - 1,  # noqa: E731
+                                  torch.rand(s, device=dev, generator=g) * 2 - 1)
+    A, B, dC = mk(32, 32, 32, 32), mk(32, 32, 32, 32), mk(32, 32, 32, 32)
+    C = torch.empty_like(dC)
+    dA, dB = torch.empty_like(A), torch.empty_like(B)
+    v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+    ctx.set_method("tc_3xtf32")
+    fwd_ms = _events_ms(torch, lambda: t1m.contract_raw(1.0, v(A), "abcd", v(B), "ebfd", 0.0,
+                                                        v(C), "aecf", t1m.FLAG_NO_TIMING, ctx),
+                        args.steps, args.warmup)
+    vjp_ms = _events_ms(torch, lambda: t1m.contract_vjp(v(dC), "aecf", v(A), "abcd", v(B),
+                                                        "ebfd", v(dA), v(dB), ctx=ctx),
+                        args.steps, args.warmup)
+    A64, B64, G64 = (z.to(torch.complex128) for z in (A, B, dC))
+    rA = torch.einsum("aecf,ebfd->abcd", G64, B64.conj())
+    rB = torch.einsum("abcd,aecf->ebfd", A64.conj(), G64)
+    eA = float((dA.to(torch.complex128) - rA).abs().max() / rA.abs().max())
+    eB = float((dB.to(torch.complex128) - rB).abs().max() / rB.abs().max())
+    flops = 8.0 * 32 ** 6
+    # Ring chain: four order-3 tensors, bond 64, physical 8, to a scalar.
+    ext = dict(a=64, b=64, c=64, d=64, p=8, q=8)
+    labels, outs = ["apb", "bpc", "cqd", "dqa"], ["ac", "aqd", ""]
+    xs = [mk(*[ext[c] for c in lab]) / 8.0 for lab in labels]
+    chain = ContractionChain(labels, outs)
+    one = torch.ones((), dtype=torch.complex64, device=dev)
+    chain_ms = _events_ms(torch, lambda: chain.backward(xs, one, ctx=ctx), 5, 2)
+    ctx.close()
+    print(json.dumps({"workload": "config5 abcd,ebfd->aecf extents 32 + VJP; ring chain",
+                      "forward_ms": fwd_ms, "forward_tflops": flops / fwd_ms / 1e9,
+                      "vjp_ms": vjp_ms, "vjp_tflops": 2 * flops / vjp_ms / 1e9,
+                      "rel_err_dA": eA, "rel_err_dB": eB,
+                      "ring_chain_backward_ms": chain_ms}), flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -388,11 +620,23 @@ def main() -> None:
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--method", default="auto")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="headline",
+                    choices=["headline", "config2", "logmag", "batch", "vjp"])
+    ap.add_argument("--items", type=int, default=1024)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "headline":
+        # The workloads run their contexts on torch's current stream and time
+        # with torch events; a created stream (not the legacy stream 0, which
+        # t1m_set_stream reads as "the context's own") keeps both on one.
+        import torch
+        fn = {"config2": workload_config2, "logmag": workload_logmag,
+              "batch": workload_batch, "vjp": workload_vjp}[args.workload]
+        with torch.cuda.stream(torch.cuda.Stream()):
+            fn(args)
     else:
         run_gpu(args)
 

@@ -368,13 +368,23 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       const float2* __restrict__ A = static_cast<const float2*>(g.A);
       const float2* __restrict__ B = static_cast<const float2*>(g.B);
       const int amode = p->amode, bmode = p->bmode;
-      // Row offsets of the four 16-row A blocks (block TMA), per tile.
-      int c0a[4] = {0, 0, 0, 0};
-      if (amode == kAMK16 && lt == 0) {
+      // Element offsets of the 16-row A blocks and 16-column B blocks of this
+      // tile (block TMA modes), per tile; rows past the edge read row 0's
+      // block (their products only reach outputs that are not written).
+      int64_t rowa[4] = {0, 0, 0, 0};
+      int64_t colb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (lt == 0 && (amode == kAMK16 || amode == kAKM16)) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int64_t m = tr.m0 + 16 * j;
-          c0a[j] = m < g.M ? static_cast<int>(2 * offs(g.rsA, g.uA_m, m)) : 0;
+          rowa[j] = m < g.M ? offs(g.rsA, g.uA_m, m) : 0;
+        }
+      }
+      if (lt == 0 && bmode == kBNK16) {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int64_t n = tr.n0 + 16 * j;
+          colb[j] = n < g.N ? offs(g.csB, g.uB_n, n) : 0;
         }
       }
       // Tiles fetched entirely by TMA need only the TMA thread; the other
@@ -421,13 +431,28 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           if (amode == kAMK16)
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-              ptx::tma_load_2d(raw_a(r) + 2048u * j, &p->map_a, c0a[j], static_cast<int>(k0), raw_full(r));
+              ptx::tma_load_2d(raw_a(r) + 2048u * j, &p->map_a, static_cast<int>(2 * rowa[j]),
+                               static_cast<int>(k0), raw_full(r));
           if (amode == kAKM)
             ptx::tma_load_2d(raw_a(r), &p->map_a, static_cast<int>(2 * offs(g.csA, g.uA_k, k0)),
                              static_cast<int>(tr.m0), raw_full(r));
+          if (amode == kAKM16) {
+            const int64_t ck = offs(g.csA, g.uA_k, k0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              ptx::tma_load_2d(raw_a(r) + 2048u * j, &p->map_a, static_cast<int>(2 * (rowa[j] + ck)),
+                               0, raw_full(r));
+          }
           if (bmode == kBNK)
             ptx::tma_load_2d(raw_b(r), &p->map_b, static_cast<int>(2 * offs(g.rsB, g.uB_k, k0)),
                              static_cast<int>(tr.n0), raw_full(r));
+          if (bmode == kBNK16) {
+            const int64_t rk = offs(g.rsB, g.uB_k, k0);
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              ptx::tma_load_2d(raw_b(r) + 2048u * j, &p->map_b, static_cast<int>(2 * (colb[j] + rk)),
+                               0, raw_full(r));
+          }
           if (bmode == kBKN)
             ptx::tma_load_2d(raw_b(r), &p->map_b, static_cast<int>(2 * tr.n0), static_cast<int>(k0), raw_full(r));
           if (!gathering) {
@@ -638,7 +663,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       using I0 = std::integral_constant<int, 0>;
       using I1 = std::integral_constant<int, 1>;
       using I2 = std::integral_constant<int, 2>;
-      const int alay = amode == kAKM ? 2 : (amode == kAMK16 ? 1 : 0);
+      const int alay = (amode == kAKM || amode == kAKM16) ? 2 : (amode == kAMK16 ? 1 : 0);
       const int blay = bmode == kBKN ? 1 : 0;
       switch (alay * 2 + blay) {
         case 0: ok = run_stages(I0{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
@@ -1197,6 +1222,33 @@ cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaS
   }
 }
 
+// Rows of every 16-aligned block of `rows` step by one common stride *stride
+// (the same for all blocks, a 16-byte multiple), and every block start plus
+// every 16-block start of `runs` is even (16-byte aligned complex64): the
+// block-scatter condition of the KM16 / NK16 modes.
+// The row coordinate of these boxes is always 0..15 and TMA bounds-checks
+// coordinates, not addresses, so every block must be a full block of valid
+// rows: n must be a multiple of 16.
+bool common_block_stride16(const std::vector<int64_t>& rows, const std::vector<int64_t>& runs,
+                           int64_t n, int64_t* stride) {
+  if (n < 16 || n % 16 != 0) return false;
+  int64_t s = -1;
+  for (int64_t b = 0; b < n; b += 16) {
+    if (rows[b] & 1) return false;
+    const int64_t e = std::min<int64_t>(n, b + 16);
+    for (int64_t i = b + 1; i < e; ++i) {
+      const int64_t d = rows[i] - rows[i - 1];
+      if (s < 0) s = d;
+      if (d != s) return false;
+    }
+  }
+  if (s <= 0 || (s * 8) % 16 != 0) return false;
+  for (size_t k = 0; k + 1 < runs.size(); k += 16)
+    if (runs[k] & 1) return false;
+  *stride = s;
+  return true;
+}
+
 std::mutex g_attr_mutex;
 bool g_attr_set = false;
 
@@ -1237,6 +1289,11 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
              make_map(&p->map_a, g.A, plan.spanA, g.M, plan.uA_m, 2 * kStepK, kTileMc, true)) {
     p->amode = kAKM;
     p->block_maps |= 1;
+  } else if (int64_t sm = 0; g.K % kStepK == 0 && unit_blocks16(plan.csA, g.K) &&
+                             common_block_stride16(plan.rsA, plan.csA, g.M, &sm) &&
+                             make_map(&p->map_a, g.A, plan.spanA, 16, sm, 2 * kStepK, 16, true)) {
+    p->amode = kAKM16;
+    p->block_maps |= 1;
   }
   // B: TMA over a uniform 2-D view or per unit-stride 16-element K block, or gather.
   p->bmode = kBGather;
@@ -1249,6 +1306,11 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
   else if (plan.uB_n >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.rsB, g.K) &&
            make_map(&p->map_b, g.B, plan.spanB, g.N, plan.uB_n, 2 * kStepK, kTileN, true)) {
     p->bmode = kBNK;
+    p->block_maps |= 2;
+  } else if (int64_t sn = 0; g.K % kStepK == 0 && unit_blocks16(plan.rsB, g.K) &&
+                             common_block_stride16(plan.csB, plan.rsB, g.N, &sn) &&
+                             make_map(&p->map_b, g.B, plan.spanB, 16, sn, 2 * kStepK, 16, true)) {
+    p->bmode = kBNK16;
     p->block_maps |= 2;
   }
   return true;

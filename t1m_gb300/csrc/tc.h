@@ -20,8 +20,12 @@ namespace gb300 {
 //   B: gather [n][k] swizzled;  NK: one TMA box [128 n][16 k] with 128 B
 //      swizzle (K unit stride, or unit-stride 16-element K blocks);
 //      KN: one TMA box [16 k][128 n] (N unit stride)
-enum : int32_t { kAGather = 0, kAMK = 1, kAMK16 = 2, kAKM = 3 };
-enum : int32_t { kBGather = 0, kBNK = 1, kBKN = 2 };
+//   A KM16 / B NK16: K runs in unit-stride 16-element blocks and rows that
+//      step by one common stride inside every 16-row block: one TMA box
+//      [16 rows][16 k] (128 B swizzle) per 16-row block, its coordinate the
+//      block's element offset; same shared-memory layouts as KM / NK.
+enum : int32_t { kAGather = 0, kAMK = 1, kAMK16 = 2, kAKM = 3, kAKM16 = 4 };
+enum : int32_t { kBGather = 0, kBNK = 1, kBKN = 2, kBNK16 = 3 };
 
 struct TcProblem {
   CUtensorMap map_a;
