@@ -297,6 +297,19 @@ def run_gpu(args) -> None:
     torch.cuda.synchronize()
     err_plain = _sampled_error(torch, ga, gb, gc)
     ms_plain, _ = timed("plain", plain_steps, 1)
+    # The other tensor-core split forms on the same workload.
+    other = {}
+    if tc_method != "plain":
+        for m in ("tc_3xtf32", "tc_bf16x3", "tc_bf16x6"):
+            if m == tc_method:
+                continue
+            one(m)
+            torch.cuda.synchronize()
+            e = _sampled_error(torch, ga, gb, gc)
+            ms_m, _ = timed(m, max(1, min(args.steps, 10)), 1)
+            other[m] = {"value": FLOPS / (ms_m / max(1, min(args.steps, 10)) * 1e-3) / 1e12,
+                        "unit": "TFLOP/s", "rel_err_max": e[0], "rel_err_fro": e[1],
+                        "meets_1e-6": e[0] <= 1e-6}
     # Per-launch kernel time of the dominant kernel, events around the launch
     # on the launching stream.
     ctx.set_method(tc_method)
@@ -355,6 +368,7 @@ def run_gpu(args) -> None:
             "plain_fp32": {"value": plain_tflops, "unit": "TFLOP/s", "steps": plain_steps,
                            "rel_err_max": err_plain[0], "rel_err_fro": err_plain[1]},
             "speedup_vs_plain": per_gpu / plain_tflops,
+            "other_tc_methods": other,
             "rel_err": {"max": err_tc[0], "fro": err_tc[1],
                         "oracle": "2048 sampled entries, FP64 dot products"},
             "roofline": {"bound": "tensor" if tc_method != "plain" else "fp32-simt",
@@ -499,9 +513,10 @@ def workload_logmag(args):
     dims = [[EXT] * 4] * 3
     ta, tb, tc = (t1m.tensor(d, x) for d, x in zip(dims, (ga, gb, gc)))
     out = []
-    for m in ("plain", "tc_3xtf32"):
+    for m in ("plain", "tc_3xtf32", "tc_bf16x3", "tc_bf16x6"):
         ctx.set_method(m)
-        rep = t1m.contract_raw(1.0, ta, LA, tb, LB, 0.0, tc, LC, 0, ctx)
+        rep = min((t1m.contract_raw(1.0, ta, LA, tb, LB, 0.0, tc, LC, 0, ctx) for _ in range(3)),
+                  key=lambda r: r.kernel_ms)
         err = _sampled_err(LA, LB, LC, dims, ga, gb, gc)
         out.append({"method": m, "ms": rep.kernel_ms, "tflops": FLOPS / rep.kernel_ms / 1e9,
                     "rel_err_max": err[0], "rel_err_fro": err[1]})
@@ -589,8 +604,10 @@ def workload_vjp(args):
                                                         v(C), "aecf", t1m.FLAG_NO_TIMING, ctx),
                         args.steps, args.warmup)
     vjp_ms = _events_ms(torch, lambda: t1m.contract_vjp(v(dC), "aecf", v(A), "abcd", v(B),
-                                                        "ebfd", v(dA), v(dB), ctx=ctx),
+                                                        "ebfd", v(dA), v(dB), ctx=ctx,
+                                                        timed=False),
                         args.steps, args.warmup)
+    vrep = t1m.contract_vjp(v(dC), "aecf", v(A), "abcd", v(B), "ebfd", v(dA), v(dB), ctx=ctx)
     A64, B64, G64 = (z.to(torch.complex128) for z in (A, B, dC))
     rA = torch.einsum("aecf,ebfd->abcd", G64, B64.conj())
     rB = torch.einsum("abcd,aecf->ebfd", A64.conj(), G64)
@@ -608,6 +625,7 @@ def workload_vjp(args):
     print(json.dumps({"workload": "config5 abcd,ebfd->aecf extents 32 + VJP; ring chain",
                       "forward_ms": fwd_ms, "forward_tflops": flops / fwd_ms / 1e9,
                       "vjp_ms": vjp_ms, "vjp_tflops": 2 * flops / vjp_ms / 1e9,
+                      "vjp_kernel_ms_reported": vrep.kernel_ms, "vjp_kernels": vrep.kernels,
                       "rel_err_dA": eA, "rel_err_dB": eB,
                       "ring_chain_backward_ms": chain_ms}), flush=True)
 

@@ -312,9 +312,12 @@ def contract_scaled(alpha, a: tensor, la: str, b: tensor, lb: str, beta, c: tens
 
 def contract_vjp(dc: tensor, lc: str, a: tensor, la: str, b: tensor, lb: str,
                  da: tensor | None = None, db: tensor | None = None,
-                 accumulate: bool = False, ctx: Context | None = None) -> Report:
+                 accumulate: bool = False, ctx: Context | None = None,
+                 timed: bool = True) -> Report:
     """Adjoint of C = A*B: dA = dC*conj(B), dB = conj(A)*dC (conjugate-Wirtinger
-    convention of PyTorch's complex autograd).  da/db may be None."""
+    convention of PyTorch's complex autograd).  da/db may be None.  With
+    timed=False the calls stay asynchronous on the context's stream (no
+    per-call events or synchronisation; the report carries no times)."""
     ctx = ctx or default_context()
     dts = {dc.dtype(), a.dtype(), b.dtype()}
     if len(dts) != 1:
@@ -327,7 +330,8 @@ def contract_vjp(dc: tensor, lc: str, a: tensor, la: str, b: tensor, lb: str,
     rep = Report()
     st = lib().t1m_contract_vjp(ctx.handle, dtype, C.byref(tdc), lc.encode(), C.byref(ta),
                                 la.encode(), C.byref(tb), lb.encode(), pda, pdb,
-                                FLAG_ACCUMULATE if accumulate else 0, C.byref(rep))
+                                (FLAG_ACCUMULATE if accumulate else 0) |
+                                (0 if timed else FLAG_NO_TIMING), C.byref(rep))
     if st != OK:
         raise T1MError(st, (lib().t1m_last_error(ctx.handle) or b"").decode())
     return rep

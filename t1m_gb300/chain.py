@@ -20,7 +20,8 @@ from __future__ import annotations
 from dataclasses import dataclass
 from typing import Sequence
 
-from . import Context, contract_raw, contract_vjp, default_context, row_major, tensor
+from . import (FLAG_NO_TIMING, Context, contract_raw, contract_vjp, default_context,
+               row_major, tensor)
 
 
 @dataclass(frozen=True)
@@ -61,7 +62,10 @@ class ContractionChain:
         st = self.steps[i]
         out = torch.empty([ext[ch] for ch in st.out], dtype=left.dtype, device=left.device)
         contract_raw(1.0, _view(left), st.left, _view(right), st.right, 0.0, _view(out), st.out,
-                     0, ctx)
+                     FLAG_NO_TIMING, ctx)
+        # The context's stream is not torch's: finish before torch may reuse
+        # or read any buffer of this step.
+        ctx.synchronize()
         return out
 
     def forward(self, xs, upto: int | None = None, ctx: Context | None = None):
@@ -87,7 +91,8 @@ class ContractionChain:
             d_left = torch.empty_like(left)
             d_right = torch.empty_like(xs[i + 1])
             contract_vjp(_view(g), st.out, _view(left), st.left, _view(xs[i + 1]), st.right,
-                         _view(d_left), _view(d_right), ctx=ctx)
+                         _view(d_left), _view(d_right), ctx=ctx, timed=False)
+            ctx.synchronize()
             grads[i + 1] = d_right
             g = d_left
             del left

@@ -151,6 +151,34 @@ __device__ __forceinline__ Split split_tf32(float x) {
   return {__float_as_uint(h), __float_as_uint(l)};
 }
 
+// Split-product precision of the one-tile-per-CTA kernel.
+//   TF32x3: x = hi + lo (TF32), products hi*hi + hi*lo + lo*hi (kind::tf32).
+//   BF16x3: x = x0 + x1 (bf16, 8 significant bits each), products
+//           x0*y0 + x0*y1 + x1*y0 (kind::f16): about 16 correct bits.
+//   BF16x6: x = x0 + x1 + x2, products x0*y0 + x0*y1 + x1*y0 + x1*y1 +
+//           x0*y2 + x2*y0: about 24 correct bits (FP32-class).
+// The bf16 forms are the split-and-sum scheme of Henry, Tang and Heinecke,
+// "Leveraging the bfloat16 artificial intelligence datatype for
+// higher-precision computations" (ARITH 2019).
+enum : int { kPrecTF32x3 = 0, kPrecBF16x3 = 1, kPrecBF16x6 = 2 };
+
+// Split a pair of floats (consecutive K) into P packed bf16x2 words: piece 0
+// is the round-to-nearest bf16 of the value, each further piece the bf16 of
+// the remainder (x - x0 is exact in FP32).  Low half = x, high half = y.
+template <int P>
+__device__ __forceinline__ void split_bf16(float x, float y, uint32_t& w0, uint32_t& w1,
+                                           uint32_t& w2) {
+  w0 = ptx::cvt_bf16x2(x, y);
+  const float rx = __fsub_rn(x, __uint_as_float(w0 << 16));
+  const float ry = __fsub_rn(y, __uint_as_float(w0 & 0xFFFF0000u));
+  w1 = ptx::cvt_bf16x2(rx, ry);
+  if (P == 3) {
+    const float sx = __fsub_rn(rx, __uint_as_float(w1 << 16));
+    const float sy = __fsub_rn(ry, __uint_as_float(w1 & 0xFFFF0000u));
+    w2 = ptx::cvt_bf16x2(sx, sy);
+  }
+}
+
 __device__ __forceinline__ float2 lds64(uint32_t addr) {
   float2 v;
   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
@@ -373,14 +401,14 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       // block (their products only reach outputs that are not written).
       int64_t rowa[4] = {0, 0, 0, 0};
       int64_t colb[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-      if (lt == 0 && (amode == kAMK16 || amode == kAKM16)) {
+      if (lt == 0 && (amode == kAMK16 || amode == kAKM16 || amode == kAMK16K)) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int64_t m = tr.m0 + 16 * j;
           rowa[j] = m < g.M ? offs(g.rsA, g.uA_m, m) : 0;
         }
       }
-      if (lt == 0 && bmode == kBNK16) {
+      if (lt == 0 && (bmode == kBNK16 || bmode == kBKN16)) {
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int64_t n = tr.n0 + 16 * j;
@@ -446,7 +474,14 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           if (bmode == kBNK)
             ptx::tma_load_2d(raw_b(r), &p->map_b, static_cast<int>(2 * offs(g.rsB, g.uB_k, k0)),
                              static_cast<int>(tr.n0), raw_full(r));
-          if (bmode == kBNK16) {
+          if (amode == kAMK16K) {
+            const int64_t ck = offs(g.csA, g.uA_k, k0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              ptx::tma_load_2d(raw_a(r) + 2048u * j, &p->map_a, static_cast<int>(2 * (rowa[j] + ck)),
+                               0, raw_full(r));
+          }
+          if (bmode == kBNK16 || bmode == kBKN16) {
             const int64_t rk = offs(g.rsB, g.uB_k, k0);
 #pragma unroll
             for (int j = 0; j < 8; ++j)
@@ -512,7 +547,8 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
     // One tile's stage loop for one (A layout, B layout) pair; the layout
     // decisions are compile-time inside, taken once per tile outside.
     //   A layouts: 0 = [k][m] rows of 512 B, 1 = four [16 k][16 m] blocks,
-    //              2 = [m][k] 128 B swizzled;  B: 0 = [n][k] swizzled, 1 = [k][n].
+    //              2 = [m][k] 128 B swizzled;  B: 0 = [n][k] swizzled, 1 = [k][n],
+    //              3 = eight [16 k][16 n] blocks.
     auto run_stages = [&](auto alay, auto blay, const TileRef& tr, bool conjA, bool conjB,
                           bool row_ok, int64_t chunk_base) -> bool {
       constexpr int AL = decltype(alay)::value;
@@ -532,12 +568,18 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         abase = static_cast<uint32_t>((8 * wg) * 512 + ci * 8);
       }
       constexpr uint32_t kAStep = AL == 1 ? 128u : 512u;
-      // B: piece j of this thread is piece 0 plus 4096 j bytes in both the raw
-      // tile and (for [n][k]) the swizzled operand tile.
-      const uint32_t bsrc0 = BL == 1 ? static_cast<uint32_t>((pt >> 6) * 1024 + 2 * (pt & 63) * 8)
-                                     : swz128(pt >> 3, 2 * (pt & 7));
+      // B: piece j of this thread is piece 0 plus kBStep j bytes in the raw
+      // tile (and for [n][k] 4096 j in the swizzled operand tile).  In the
+      // [k][n] forms piece j is k = (pt >> 6) + 4 j, columns n, n + 1.
+      constexpr bool kBRowsK = BL == 1 || BL == 3;
+      constexpr uint32_t kBStep = BL == 3 ? 512u : 4096u;
+      const int bn = 2 * (pt & 63), bk = pt >> 6;
+      const uint32_t bsrc0 =
+          BL == 1 ? static_cast<uint32_t>(bk * 1024 + bn * 8)
+          : BL == 3 ? static_cast<uint32_t>((bn >> 4) * 2048 + bk * 128 + (bn & 15) * 8)
+                    : swz128(pt >> 3, 2 * (pt & 7));
       uint32_t boff_kn[4][2];
-      if constexpr (BL == 1) {
+      if constexpr (kBRowsK) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
           const int k = (pt >> 6) + 4 * j, n = 2 * (pt & 63);
@@ -568,7 +610,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         float4 bv[4];
         const uint32_t b0 = rb + bsrc0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bv[j] = lds128(b0 + 4096u * j);
+        for (int j = 0; j < 4; ++j) bv[j] = lds128(b0 + kBStep * j);
         __syncwarp();
         if (lane == 0) ptx::mbar_arrive(raw_empty(rr));
         if (++rr == kRaw) {
@@ -610,7 +652,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           }
           const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
           const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
-          if constexpr (BL == 1) {
+          if constexpr (kBRowsK) {
             sts64(ob + boff_kn[j][0], r0.hi, i0.hi);
             sts64(ob + boff_kn[j][1], r1.hi, i1.hi);
             sts64(ob + kBHalfBytes + boff_kn[j][0], r0.lo, i0.lo);
@@ -663,15 +705,20 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       using I0 = std::integral_constant<int, 0>;
       using I1 = std::integral_constant<int, 1>;
       using I2 = std::integral_constant<int, 2>;
-      const int alay = (amode == kAKM || amode == kAKM16) ? 2 : (amode == kAMK16 ? 1 : 0);
-      const int blay = bmode == kBKN ? 1 : 0;
-      switch (alay * 2 + blay) {
+      using I3 = std::integral_constant<int, 3>;
+      const int alay = (amode == kAKM || amode == kAKM16) ? 2
+                       : (amode == kAMK16 || amode == kAMK16K) ? 1 : 0;
+      const int blay = bmode == kBKN ? 1 : (bmode == kBKN16 ? 3 : 0);
+      switch (alay * 4 + blay) {
         case 0: ok = run_stages(I0{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
         case 1: ok = run_stages(I0{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 2: ok = run_stages(I1{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 3: ok = run_stages(I1{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 4: ok = run_stages(I2{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        default: ok = run_stages(I2{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 3: ok = run_stages(I0{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 4: ok = run_stages(I1{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 5: ok = run_stages(I1{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 7: ok = run_stages(I1{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 8: ok = run_stages(I2{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        case 9: ok = run_stages(I2{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        default: ok = run_stages(I2{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
       }
       if (!ok) break;
 
@@ -761,9 +808,17 @@ struct TmaMaps {
   CUtensorMap b;
 };
 
-template <int AMode, int BMode>
+// Prec selects the split products (kPrec*).  The bf16 forms keep the same
+// tiles, stages and accumulators; per stage (32 real K) they issue two K = 16
+// kind::f16 MMAs per product, A pieces packed two per TMEM column (16 columns
+// each) and B pieces in 64-byte halves of the 128-byte swizzled rows (pieces
+// 0 | 1 in the first B buffer, piece 2 in the second).
+template <int AMode, int BMode, int Prec>
 __global__ void __launch_bounds__(kThreads, 1)
-tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
+tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
+  constexpr bool kBF16 = Prec != kPrecTF32x3;
+  constexpr int kPieces = Prec == kPrecBF16x6 ? 3 : 2;
+  constexpr uint32_t kIdescP = kBF16 ? ptx::idesc_f32acc(1u /*BF16*/, 128, kTileN) : kIdesc;
   constexpr bool kTmaA = AMode != kGatherMK;
   constexpr bool kTmaB = BMode != kGatherNK;
   constexpr bool kGather = !kTmaA || !kTmaB;
@@ -860,17 +915,39 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
         ptx::tc_fence_after();
         const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
         const uint32_t d_corr = tmem + kCorrCol;
-        const uint32_t a_hi = tmem + kAStageCol + 64u * st;
-        const uint32_t a_lo = a_hi + 32u;
-        const uint32_t b_hi = op0 + st * kOpBytes;
-        const uint32_t b_lo = b_hi + kBHalfBytes;
+        if constexpr (!kBF16) {
+          const uint32_t a_hi = tmem + kAStageCol + 64u * st;
+          const uint32_t a_lo = a_hi + 32u;
+          const uint32_t b_hi = op0 + st * kOpBytes;
+          const uint32_t b_lo = b_hi + kBHalfBytes;
 #pragma unroll
-        for (int kk = 0; kk < 4; ++kk) {
-          const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
-          const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
-          ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
-          ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
-          ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
+          for (int kk = 0; kk < 4; ++kk) {
+            const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
+            const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
+            ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
+            ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
+            ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
+          }
+        } else {
+          // A piece p: 16 TMEM columns at +16p; B piece p: 64-byte half
+          // (p & 1) of the rows of B buffer (p >> 1).  K = 16 per MMA.
+          const uint32_t a0 = tmem + kAStageCol + 64u * st;
+          const uint32_t bb = op0 + st * kOpBytes;
+#pragma unroll
+          for (int kk = 0; kk < 2; ++kk) {
+            auto bd = [&](int p) {
+              return ptx::smem_desc_sw128(bb + (p >> 1) * kBHalfBytes + 64u * (p & 1) + 32u * kk);
+            };
+            const uint32_t ak = a0 + 8u * kk;
+            ptx::mma_f16_ts(d_main, ak, bd(0), kIdescP, (chunk_start && kk == 0) ? 0u : 1u);
+            ptx::mma_f16_ts(d_corr, ak, bd(1), kIdescP, (s == 0 && kk == 0) ? 0u : 1u);
+            ptx::mma_f16_ts(d_corr, ak + 16u, bd(0), kIdescP, 1u);
+            if (kPieces == 3) {
+              ptx::mma_f16_ts(d_corr, ak + 16u, bd(1), kIdescP, 1u);
+              ptx::mma_f16_ts(d_corr, ak, bd(2), kIdescP, 1u);
+              ptx::mma_f16_ts(d_corr, ak + 32u, bd(0), kIdescP, 1u);
+            }
+          }
         }
         ptx::mma_commit(empty_bar(st));
         if ((s % kFold) == kFold - 1 || s == ksteps - 1) ptx::mma_commit(chunk_full(buf));
@@ -983,6 +1060,20 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
         boff[j][1] = 0;
       }
     }
+    // bf16 B: id = pt + 256 j covers column n = id & 127 and complex k
+    // 4 kq .. 4 kq + 3 (kq = id >> 7): two 16-byte raw reads (one per k pair)
+    // in the swizzled [n][k] tiles, four 8-byte reads in the [k][n] tile;
+    // one 16-byte chunk (8 bf16) per piece, chunk kq (+4 for odd pieces) of
+    // row n.  Consecutive lanes take consecutive n: no bank conflicts.
+    uint32_t b16src[2], b16row[2], b16chunk[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int id = pt + 256 * j;
+      const int n = id & 127, kq = id >> 7;
+      b16src[j] = (BMode == kTmaKN) ? static_cast<uint32_t>(4 * kq * 1024 + n * 8) : swz128(n, 4 * kq);
+      b16row[j] = static_cast<uint32_t>((n >> 3) * 1024 + (n & 7) * 128);
+      b16chunk[j] = static_cast<uint32_t>(kq ^ (n & 7));
+    }
 
     bool ok = true;
     int r = 0, st = 0;
@@ -1009,8 +1100,24 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
       }
       // B: four 16-byte pieces (two complex each) of the raw tile.
       float4 bv[4];
+      if constexpr (!kBF16) {
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
+        for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          if (BMode == kTmaKN) {
+            const float2 t0 = lds64(rb + b16src[j]), t1 = lds64(rb + b16src[j] + 1024u);
+            const float2 t2 = lds64(rb + b16src[j] + 2048u), t3 = lds64(rb + b16src[j] + 3072u);
+            bv[2 * j] = make_float4(t0.x, t0.y, t1.x, t1.y);
+            bv[2 * j + 1] = make_float4(t2.x, t2.y, t3.x, t3.y);
+          } else {
+            // k pair 2kq + 1 sits in the neighbouring 16-byte chunk (bit 4).
+            bv[2 * j] = lds128(rb + b16src[j]);
+            bv[2 * j + 1] = lds128(rb + (b16src[j] ^ 16u));
+          }
+        }
+      }
       __syncwarp();
       if (lane == 0) ptx::mbar_arrive(raw_empty(r));
 
@@ -1020,43 +1127,82 @@ tc3xtf32_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int
         break;
       }
       ptx::tc_fence_after();
-      // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
-      uint32_t hi[16], lo[16];
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        float2 v = av[j];
-        if (conjA) v.y = -v.y;
-        if (!row_ok) v = make_float2(0.f, 0.f);
-        const float x0 = part ? v.y : v.x;
-        const float x1 = part ? v.x : -v.y;
-        const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
-        hi[2 * j] = s0.hi;
-        lo[2 * j] = s0.lo;
-        hi[2 * j + 1] = s1.hi;
-        lo[2 * j + 1] = s1.lo;
-      }
-      const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 16u * wg;
-      ptx::tmem_st16(a_col, hi);
-      ptx::tmem_st16(a_col + 32u, lo);
-      // B -> shared memory (swizzled K-major hi and lo tiles).
       const uint32_t ob = op0 + st * kOpBytes;
+      if constexpr (kBF16) {
+        // A -> TMEM: the 1M row pairs of this thread's 8 complex k, split
+        // into kPieces bf16x2 words each; piece p at columns +16p (+8 for
+        // the second half of the K-step).
+        uint32_t w[3][8];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        float4 v = bv[j];
-        if (conjB) {
-          v.y = -v.y;
-          v.w = -v.w;
+        for (int j = 0; j < 8; ++j) {
+          float2 v = av[j];
+          if (conjA) v.y = -v.y;
+          if (!row_ok) v = make_float2(0.f, 0.f);
+          const float x0 = part ? v.y : v.x;
+          const float x1 = part ? v.x : -v.y;
+          split_bf16<kPieces>(x0, x1, w[0][j], w[1][j], w[2][j]);
         }
-        const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
-        const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
-        if (BMode == kTmaKN) {
-          sts64(ob + boff[j][0], r0.hi, i0.hi);
-          sts64(ob + boff[j][1], r1.hi, i1.hi);
-          sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
-          sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
-        } else {
-          sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
-          sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+        const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 8u * wg;
+#pragma unroll
+        for (int p = 0; p < kPieces; ++p) ptx::tmem_st8(a_col + 16u * p, w[p]);
+        // B -> shared memory: 4 complex k of column n, re/im interleaved.
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          float4 v0 = bv[2 * j], v1 = bv[2 * j + 1];
+          if (conjB) {
+            v0.y = -v0.y;
+            v0.w = -v0.w;
+            v1.y = -v1.y;
+            v1.w = -v1.w;
+          }
+          uint32_t q[4][3];
+          split_bf16<kPieces>(v0.x, v0.y, q[0][0], q[0][1], q[0][2]);
+          split_bf16<kPieces>(v0.z, v0.w, q[1][0], q[1][1], q[1][2]);
+          split_bf16<kPieces>(v1.x, v1.y, q[2][0], q[2][1], q[2][2]);
+          split_bf16<kPieces>(v1.z, v1.w, q[3][0], q[3][1], q[3][2]);
+#pragma unroll
+          for (int p = 0; p < kPieces; ++p)
+            sts128(ob + (p >> 1) * kBHalfBytes + b16row[j] + ((b16chunk[j] ^ (4u * (p & 1))) << 4),
+                   q[0][p], q[1][p], q[2][p], q[3][p]);
+        }
+      } else {
+        // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
+        uint32_t hi[16], lo[16];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          float2 v = av[j];
+          if (conjA) v.y = -v.y;
+          if (!row_ok) v = make_float2(0.f, 0.f);
+          const float x0 = part ? v.y : v.x;
+          const float x1 = part ? v.x : -v.y;
+          const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
+          hi[2 * j] = s0.hi;
+          lo[2 * j] = s0.lo;
+          hi[2 * j + 1] = s1.hi;
+          lo[2 * j + 1] = s1.lo;
+        }
+        const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 16u * wg;
+        ptx::tmem_st16(a_col, hi);
+        ptx::tmem_st16(a_col + 32u, lo);
+        // B -> shared memory (swizzled K-major hi and lo tiles).
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          float4 v = bv[j];
+          if (conjB) {
+            v.y = -v.y;
+            v.w = -v.w;
+          }
+          const Split r0 = split_tf32(v.x), i0 = split_tf32(v.y);
+          const Split r1 = split_tf32(v.z), i1 = split_tf32(v.w);
+          if (BMode == kTmaKN) {
+            sts64(ob + boff[j][0], r0.hi, i0.hi);
+            sts64(ob + boff[j][1], r1.hi, i1.hi);
+            sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
+            sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
+          } else {
+            sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
+            sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+          }
         }
       }
       ptx::tmem_wait_st();
@@ -1198,27 +1344,37 @@ bool unit_blocks16(const std::vector<int64_t>& v, int64_t n) {
   return true;
 }
 
-template <int AMode, int BMode>
+template <int AMode, int BMode, int Prec>
 cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
                          int* err_flag, dim3 tiles) {
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc3xtf32_contract<AMode, BMode>,
+    cudaError_t e = cudaFuncSetAttribute(tc1m_contract<AMode, BMode, Prec>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  tc3xtf32_contract<AMode, BMode><<<tiles, kThreads, kSmemBytes, stream>>>(args, maps, err_flag);
+  tc1m_contract<AMode, BMode, Prec><<<tiles, kThreads, kSmemBytes, stream>>>(args, maps, err_flag);
   return cudaGetLastError();
 }
 
-template <int AMode>
+template <int AMode, int Prec>
 cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
                      int* err_flag, dim3 tiles) {
   switch (bmode) {
-    case kTmaNK: return launch_modes<AMode, kTmaNK>(args, maps, stream, err_flag, tiles);
-    case kTmaKN: return launch_modes<AMode, kTmaKN>(args, maps, stream, err_flag, tiles);
-    default: return launch_modes<AMode, kGatherNK>(args, maps, stream, err_flag, tiles);
+    case kTmaNK: return launch_modes<AMode, kTmaNK, Prec>(args, maps, stream, err_flag, tiles);
+    case kTmaKN: return launch_modes<AMode, kTmaKN, Prec>(args, maps, stream, err_flag, tiles);
+    default: return launch_modes<AMode, kGatherNK, Prec>(args, maps, stream, err_flag, tiles);
+  }
+}
+
+template <int Prec>
+cudaError_t launch_a(int amode, int bmode, const GemmArgs& args, const TmaMaps& maps,
+                     cudaStream_t stream, int* err_flag, dim3 tiles) {
+  switch (amode) {
+    case kTmaMK: return launch_b<kTmaMK, Prec>(bmode, args, maps, stream, err_flag, tiles);
+    case kTmaKM: return launch_b<kTmaKM, Prec>(bmode, args, maps, stream, err_flag, tiles);
+    default: return launch_b<kGatherMK, Prec>(bmode, args, maps, stream, err_flag, tiles);
   }
 }
 
@@ -1262,7 +1418,9 @@ void tc_tile(int* bm, int* bn, int* bk) {
 
 bool tc_supported(int method, int dtype, const HostPlan& plan) {
   (void)plan;
-  return method == T1M_METHOD_TC_3XTF32 && dtype == T1M_COMPLEX64;
+  return (method == T1M_METHOD_TC_3XTF32 || method == T1M_METHOD_TC_BF16X3 ||
+          method == T1M_METHOD_TC_BF16X6) &&
+         dtype == T1M_COMPLEX64;
 }
 
 bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p) {
@@ -1294,6 +1452,11 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
                              make_map(&p->map_a, g.A, plan.spanA, 16, sm, 2 * kStepK, 16, true)) {
     p->amode = kAKM16;
     p->block_maps |= 1;
+  } else if (int64_t sk = 0; g.M % 16 == 0 && unit_blocks16(plan.rsA, g.M) &&
+                             common_block_stride16(plan.csA, plan.rsA, g.K, &sk) &&
+                             make_map(&p->map_a, g.A, plan.spanA, 16, sk, 32, 16, false)) {
+    p->amode = kAMK16K;
+    p->block_maps |= 1;
   }
   // B: TMA over a uniform 2-D view or per unit-stride 16-element K block, or gather.
   p->bmode = kBGather;
@@ -1311,6 +1474,11 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
                              common_block_stride16(plan.csB, plan.rsB, g.N, &sn) &&
                              make_map(&p->map_b, g.B, plan.spanB, 16, sn, 2 * kStepK, 16, true)) {
     p->bmode = kBNK16;
+    p->block_maps |= 2;
+  } else if (int64_t sk = 0; g.N % 16 == 0 && unit_blocks16(plan.csB, g.N) &&
+                             common_block_stride16(plan.rsB, plan.csB, g.K, &sk) &&
+                             make_map(&p->map_b, g.B, plan.spanB, 16, sk, 32, 16, false)) {
+    p->bmode = kBKN16;
     p->block_maps |= 2;
   }
   return true;
@@ -1369,19 +1537,30 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   p.dep = -1;
   cudaError_t e;
-  if (p.block_maps == 0 && p.amode != kAMK16) {
-    // Uniform or gathered operands: the one-tile-per-CTA form.
+  const bool bf16 = method != T1M_METHOD_TC_3XTF32;
+  if (bf16 || (p.block_maps == 0 && p.amode != kAMK16)) {
+    // Uniform or gathered operands: the one-tile-per-CTA form.  The bf16
+    // forms exist only here: an operand that needs a per-block map is
+    // gathered instead.
     TmaMaps maps;
     maps.a = p.map_a;
     maps.b = p.map_b;
     const dim3 grid(static_cast<unsigned>(int64_t(p.tiles_m) * p.tiles_n),
                     static_cast<unsigned>(splits));
-    const int am = p.amode == kAMK ? kTmaMK : (p.amode == kAKM ? kTmaKM : kGatherMK);
-    const int bm = p.bmode == kBNK ? kTmaNK : (p.bmode == kBKN ? kTmaKN : kGatherNK);
-    switch (am) {
-      case kTmaMK: e = launch_b<kTmaMK>(bm, args, maps, stream, err_flag, grid); break;
-      case kTmaKM: e = launch_b<kTmaKM>(bm, args, maps, stream, err_flag, grid); break;
-      default: e = launch_b<kGatherMK>(bm, args, maps, stream, err_flag, grid); break;
+    const bool a_uniform = !(p.block_maps & 1);
+    const bool b_uniform = !(p.block_maps & 2);
+    const int am = (a_uniform && p.amode == kAMK) ? kTmaMK
+                   : (a_uniform && p.amode == kAKM) ? kTmaKM : kGatherMK;
+    const int bm = (b_uniform && p.bmode == kBNK) ? kTmaNK
+                   : (b_uniform && p.bmode == kBKN) ? kTmaKN : kGatherNK;
+    switch (method) {
+      case T1M_METHOD_TC_BF16X3:
+        e = launch_a<kPrecBF16x3>(am, bm, args, maps, stream, err_flag, grid);
+        break;
+      case T1M_METHOD_TC_BF16X6:
+        e = launch_a<kPrecBF16x6>(am, bm, args, maps, stream, err_flag, grid);
+        break;
+      default: e = launch_a<kPrecTF32x3>(am, bm, args, maps, stream, err_flag, grid); break;
     }
   } else {
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);

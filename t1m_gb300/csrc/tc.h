@@ -24,8 +24,13 @@ namespace gb300 {
 //      step by one common stride inside every 16-row block: one TMA box
 //      [16 rows][16 k] (128 B swizzle) per 16-row block, its coordinate the
 //      block's element offset; same shared-memory layouts as KM / NK.
-enum : int32_t { kAGather = 0, kAMK = 1, kAMK16 = 2, kAKM = 3, kAKM16 = 4 };
-enum : int32_t { kBGather = 0, kBNK = 1, kBKN = 2, kBNK16 = 3 };
+//   A MK16K / B KN16: the transposed case (adjoint operands): rows (M or N)
+//      in unit-stride 16-element blocks, K stepping by one common stride
+//      inside every 16-element K block: one box [16 k][16 rows] per 16-row
+//      block and K step, coordinate = row block offset + K block offset.
+//      A keeps the MK16 layout; B lands as eight [16 k][16 n] blocks.
+enum : int32_t { kAGather = 0, kAMK = 1, kAMK16 = 2, kAKM = 3, kAKM16 = 4, kAMK16K = 5 };
+enum : int32_t { kBGather = 0, kBNK = 1, kBKN = 2, kBNK16 = 3, kBKN16 = 4 };
 
 struct TcProblem {
   CUtensorMap map_a;
