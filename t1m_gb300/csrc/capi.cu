@@ -654,7 +654,52 @@ extern "C" int t1m_contract_vjp(t1m_context* ctx, int dtype, const t1m_tensor* d
 
 namespace {
 
-enum Family : int { kFamTC = 0, kFamSimt = 1, kFamSimtSkinny = 2 };
+enum Family : int { kFamTC = 0, kFamSimt = 1, kFamSimtSkinny = 2, kFamReduce = 3 };
+
+// Split-K inside a grouped launch: every tile covers at most kGroupKCap
+// complex (or real) K, so one long-K item (a skinny output over a big
+// contracted bundle) spreads over many CTAs instead of leaving a tail of
+// serial tiles; partials go to the group's workspace and one reduction per
+// dependency level applies the epilogues.
+constexpr int64_t kGroupKCap = 1024;
+constexpr size_t kGroupWorkBytes = size_t(2) << 30;
+constexpr size_t kGroupItemWorkBytes = size_t(256) << 20;
+
+int group_splits(int dtype, int fam, const HostPlan& hp, size_t es, int64_t* k_per_split) {
+  int bm = 0, bn = 0, bk = 0;
+  if (fam == kFamTC) {
+    tc_tile(&bm, &bn, &bk);
+  } else {
+    simt_tile(dtype, &bm, &bn, &bk);
+    if (fam == kFamSimtSkinny) bk = 16;
+  }
+  const int64_t ksteps = std::max<int64_t>(1, (hp.K + bk - 1) / bk);
+  const int64_t cap_steps = std::max<int64_t>(1, kGroupKCap / bk);
+  int64_t s = (ksteps + cap_steps - 1) / cap_steps;
+  s = std::max<int64_t>(1, std::min<int64_t>(s, 4096));
+  while (s > 1 && size_t(s) * size_t(hp.M) * size_t(hp.N) * es > kGroupItemWorkBytes) --s;
+  const int64_t steps_per = (ksteps + s - 1) / s;
+  *k_per_split = steps_per * bk;
+  return static_cast<int>((ksteps + steps_per - 1) / steps_per);
+}
+
+// Arguments of the main kernel of a split item: raw partial products (alpha 1,
+// beta 0) into `splits` dense M x N slices of `work`, m fastest.
+GemmArgs split_args(const GemmArgs& a, void* work, int64_t k_per_split) {
+  GemmArgs w = a;
+  w.C = work;
+  w.rsC = nullptr;
+  w.csC = nullptr;
+  w.uC_m = 1;
+  w.uC_n = a.M;
+  w.alpha[0] = 1.0;
+  w.alpha[1] = 0.0;
+  w.beta[0] = w.beta[1] = 0.0;
+  w.flags = (a.flags & (kFlagConjA | kFlagConjB)) | kFlagBetaZero;
+  w.k_per_split = k_per_split;
+  w.c_split_stride = a.M * a.N;
+  return w;
+}
 
 // Autotuner cache: shape class -> family, measured once per process and
 // persisted to a small versioned text file (T1M_TUNE_CACHE, default
@@ -735,6 +780,8 @@ struct t1m_group {
   void* tc_dev = nullptr;       // TcProblem array
   int* done = nullptr;          // tile-completion counters (single TC launch)
   void* simt_dev = nullptr;     // SimtProblem arrays, per (level, family)
+  void* reduce_dev = nullptr;   // SplitReduce arrays, per level
+  void* work = nullptr;         // split-K partials of all split items
   struct Launch {
     int family;
     int64_t offset;   // first descriptor in tc_dev / simt_dev
@@ -769,6 +816,10 @@ int enqueue_group(t1m_group* g, cudaStream_t s) {
         if (l.family == kFamTC)
           e = tc_launch_persistent(nullptr, static_cast<const TcProblem*>(g->tc_dev) + l.offset,
                                    l.count, l.tiles, ctx->num_sms, nullptr, s, ctx->d_err);
+        else if (l.family == kFamReduce)
+          e = launch_splitk_reduce_group(g->dtype,
+                                         static_cast<const SplitReduce*>(g->reduce_dev) + l.offset,
+                                         l.count, l.tiles, s);
         else
           e = launch_simt_group(g->dtype, l.family == kFamSimtSkinny,
                                 static_cast<const SimtProblem*>(g->simt_dev) + l.offset, l.count,
@@ -796,6 +847,8 @@ extern "C" int t1m_group_destroy(t1m_group* g) {
   if (g->vectors) cudaFree(g->vectors);
   if (g->tc_dev) cudaFree(g->tc_dev);
   if (g->simt_dev) cudaFree(g->simt_dev);
+  if (g->reduce_dev) cudaFree(g->reduce_dev);
+  if (g->work) cudaFree(g->work);
   if (g->done) cudaFree(g->done);
   delete g;
   return T1M_OK;
@@ -914,15 +967,17 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
       }
       std::vector<int> cands = {kFamSimt, kFamSimtSkinny};
       if (dtype == T1M_COMPLEX64 && ctx->method != T1M_METHOD_PLAIN) cands.push_back(kFamTC);
+      // Each candidate runs with its own split count (the main kernel only:
+      // the reduction is the same for all of them) into a scratch output.
+      size_t scratch_bytes = 0;
+      for (int f : cands) {
+        int64_t kps = 0;
+        const int sp = group_splits(dtype, f, hp, es, &kps);
+        scratch_bytes = std::max(scratch_bytes, size_t(sp) * size_t(hp.M) * size_t(hp.N) * es);
+      }
       void* scratch = nullptr;
-      if (cudaMalloc(&scratch, size_t(hp.M) * size_t(hp.N) * es) != cudaSuccess)
+      if (cudaMalloc(&scratch, scratch_bytes) != cudaSuccess)
         return fail(ctx, T1M_ERR_ALLOC, "autotune scratch");
-      GemmArgs probe = args[i];
-      probe.C = scratch;
-      probe.rsC = probe.csC = nullptr;
-      probe.uC_m = 1;
-      probe.uC_n = hp.M;
-      probe.flags = (probe.flags & (kFlagConjA | kFlagConjB)) | kFlagBetaZero;
       void* pd = nullptr;
       if (cudaMalloc(&pd, sizeof(TcProblem) > sizeof(SimtProblem) ? sizeof(TcProblem) : sizeof(SimtProblem)) != cudaSuccess) {
         cudaFree(scratch);
@@ -933,12 +988,15 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
       for (int f : cands) {
         float total = 0;
         bool ok = true;
+        int64_t kps = 0;
+        const int nsp = group_splits(dtype, f, hp, es, &kps);
+        const GemmArgs probe = split_args(args[i], scratch, kps);
         for (int rep = 0; rep < 3 && ok; ++rep) {
           cudaEventRecord(ctx->ev[4], ctx->stream);
           cudaError_t le;
           if (f == kFamTC) {
             TcProblem tp;
-            ok = tc_prepare(probe, hp, 1, &tp);
+            ok = tc_prepare(probe, hp, nsp, &tp);
             tp.tile_begin = 0;
             tp.dep = -1;
             le = ok ? tc_launch_persistent(&tp, nullptr, 1, tc_problem_tiles(tp), ctx->num_sms,
@@ -949,7 +1007,7 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
             cudaMemcpy(pd, &sp, sizeof(sp), cudaMemcpyHostToDevice);
             int bm, bn;
             simt_group_tile(dtype, f == kFamSimtSkinny, &bm, &bn);
-            const int64_t tiles = ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
+            const int64_t tiles = nsp * ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
             le = launch_simt_group(dtype, f == kFamSimtSkinny, static_cast<SimtProblem*>(pd), 1,
                                    tiles, ctx->stream);
           }
@@ -978,15 +1036,46 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
     if (changed) g_tune.save();
   }
 
+  // Split-K per item (bounded K per tile) and the workspace of the split
+  // items; if the workspace would exceed its budget the caps are relaxed.
+  std::vector<int> splits(n, 1);
+  std::vector<int64_t> kps(n, 0), work_off(n, -1);
+  size_t work_bytes = 0;
+  for (int i = 0; i < n; ++i) {
+    const HostPlan& hp = plans[i];
+    if (hp.M == 0 || hp.N == 0 || hp.K == 0) continue;
+    splits[i] = group_splits(dtype, family[i], hp, es, &kps[i]);
+    if (splits[i] > 1) {
+      work_off[i] = static_cast<int64_t>(work_bytes);
+      work_bytes += (size_t(splits[i]) * size_t(hp.M) * size_t(hp.N) * es + 255) & ~size_t(255);
+    }
+  }
+  if (work_bytes > kGroupWorkBytes) {
+    std::fill(splits.begin(), splits.end(), 1);
+    work_bytes = 0;
+  }
+  bool any_split = false;
+  for (int i = 0; i < n; ++i) any_split = any_split || splits[i] > 1;
+  if (work_bytes) {
+    e = cudaMalloc(&g->work, work_bytes);
+    if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group split-K workspace");
+  }
+  std::vector<GemmArgs> main_args(args);
+  for (int i = 0; i < n; ++i)
+    if (splits[i] > 1)
+      main_args[i] = split_args(args[i], static_cast<char*>(g->work) + work_off[i], kps[i]);
+
   // Launch lists.  One persistent tensor-core launch for everything if every
-  // item is a tensor-core item (dependencies resolved in the kernel),
-  // otherwise one launch per (level, family).
-  bool all_tc = n > 0;
+  // item is an unsplit tensor-core item (dependencies resolved in the
+  // kernel), otherwise per level one launch per family, then one grouped
+  // split-K reduction.
+  bool all_tc = n > 0 && !any_split;
   for (int i = 0; i < n; ++i) all_tc = all_tc && family[i] == kFamTC;
   int max_level = 0;
   for (int i = 0; i < n; ++i) max_level = std::max(max_level, level[i]);
   std::vector<TcProblem> tcs;
   std::vector<SimtProblem> simts;
+  std::vector<SplitReduce> reds;
   std::vector<int> tc_index(n, -1);
   g->levels.assign(max_level + 1, {});
   for (int lv = 0; lv <= max_level; ++lv) {
@@ -997,7 +1086,7 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
         const HostPlan& hp = plans[i];
         if (fam == kFamTC) {
           TcProblem tp;
-          if (!tc_prepare(args[i], hp, 1, &tp))
+          if (!tc_prepare(main_args[i], hp, splits[i], &tp))
             return fail(ctx, T1M_ERR_UNSUPPORTED, "group item " + std::to_string(i) +
                                                       " cannot run on the tensor cores");
           tp.tile_begin = (all_tc ? g->tc_total : L.tiles);
@@ -1016,14 +1105,27 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
         } else {
           int bm, bn;
           simt_group_tile(dtype, fam == kFamSimtSkinny, &bm, &bn);
-          SimtProblem sp{args[i], L.tiles};
-          L.tiles += ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
+          SimtProblem sp{main_args[i], L.tiles};
+          L.tiles += splits[i] * ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
           simts.push_back(sp);
         }
         ++L.count;
       }
       if (L.count > 0) g->levels[lv].push_back(L);
     }
+    t1m_group::Launch R{kFamReduce, int64_t(reds.size()), 0, 0};
+    for (int i = 0; i < n; ++i) {
+      if (level[i] != lv || splits[i] <= 1) continue;
+      SplitReduce r{};
+      r.out = args[i];
+      r.work = static_cast<char*>(g->work) + work_off[i];
+      r.begin = R.tiles;
+      r.splits = splits[i];
+      R.tiles += plans[i].M * plans[i].N;
+      reds.push_back(r);
+      ++R.count;
+    }
+    if (R.count > 0) g->levels[lv].push_back(R);
   }
   g->single_tc = all_tc && max_level > 0;
   g->tc_count = static_cast<int>(tcs.size());
@@ -1033,6 +1135,13 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
     if (e == cudaSuccess)
       e = cudaMemcpy(g->tc_dev, tcs.data(), tcs.size() * sizeof(TcProblem), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc(&g->done, sizeof(int) * tcs.size());
+    if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group descriptors");
+  }
+  if (!reds.empty()) {
+    e = cudaMalloc(&g->reduce_dev, reds.size() * sizeof(SplitReduce));
+    if (e == cudaSuccess)
+      e = cudaMemcpy(g->reduce_dev, reds.data(), reds.size() * sizeof(SplitReduce),
+                     cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group descriptors");
   }
   if (!simts.empty()) {

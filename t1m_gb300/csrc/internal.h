@@ -84,7 +84,9 @@ cudaError_t launch_simt(int dtype, const GemmArgs& args, int splits, cudaStream_
 void simt_tile(int dtype, int* bm, int* bn, int* bk);
 
 // One contraction of a grouped plain launch (device array, sorted by
-// tile_begin; no split-K).
+// tile_begin).  Its tiles are numbered split-major: g.k_per_split and
+// g.c_split_stride describe split-K exactly as for a single launch, and the
+// problem owns splits x tiles of the launch's tile list.
 struct SimtProblem {
   GemmArgs g;
   int64_t tile_begin;
@@ -99,6 +101,18 @@ cudaError_t launch_simt_group(int dtype, bool skinny, const SimtProblem* dev, in
 // in FP64.  W holds `splits` dense M x N partials, m fastest, of the dtype.
 cudaError_t launch_splitk_reduce(int dtype, const void* work, int splits, const GemmArgs& out,
                                  cudaStream_t stream);
+
+// Grouped split-K reduction: one launch over the outputs of many split
+// contractions (device array sorted by begin = prefix sum of M*N).
+struct SplitReduce {
+  GemmArgs out;       // C, its scatter vectors and the epilogue
+  const void* work;   // splits dense M x N partials, m fastest
+  int64_t begin;      // first output element of this problem in the launch
+  int32_t splits;
+  int32_t pad;
+};
+cudaError_t launch_splitk_reduce_group(int dtype, const SplitReduce* dev, int n,
+                                       int64_t total, cudaStream_t stream);
 
 }  // namespace gb300
 }  // namespace t1m

@@ -159,19 +159,15 @@ int build_plan(int dtype, int na, const int64_t* ea, const int64_t* sa,
     }
   }
 
-  // Mode order: M follows A, N follows B; K follows whichever operand has a
-  // unit-stride contracted mode (A first).
+  // Mode order: M follows A, N follows B; K follows B whenever B has a
+  // unit-stride contracted mode, else A.  When both have one (but different
+  // ones) the operand in the other order is gathered element by element, and
+  // the B tile (128 columns) is twice the A tile (64 rows) in the complex64
+  // kernels, so B keeps its contiguous K runs.
   order_modes(&plan->modes_m, false);
   order_modes(&plan->modes_n, false);
   bool k_by_b = false;
-  {
-    bool a_unit = false, b_unit = false;
-    for (const Mode& m : plan->modes_k) {
-      a_unit |= (m.s0 == 1 && m.extent > 1);
-      b_unit |= (m.s1 == 1 && m.extent > 1);
-    }
-    k_by_b = !a_unit && b_unit;
-  }
+  for (const Mode& m : plan->modes_k) k_by_b |= (m.s1 == 1 && m.extent > 1);
   order_modes(&plan->modes_k, k_by_b);
 
   plan->rsA = scatter(plan->modes_m, false);

@@ -129,17 +129,23 @@ simt_contract(const GemmArgs args0, const SimtProblem* group, int nprob) {
   const T* __restrict__ A = static_cast<const T*>(args.A);
   const T* __restrict__ B = static_cast<const T*>(args.B);
   const int64_t M = args.M, N = args.N;
-  // Split-K: this CTA row covers K range [kb, K); a split writes its partial
-  // product to its own slice of the workspace.
-  const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
+  const int64_t tiles_m = (M + BM - 1) / BM;
+  const int64_t tiles_n = (N + BN - 1) / BN;
+  // Split-K: this CTA covers K range [kb, K); a split writes its partial
+  // product to its own slice of the workspace.  The split is blockIdx.y for
+  // single launches; grouped launches number a problem's tiles split-major.
+  int64_t split = blockIdx.y;
+  if constexpr (kGroup) {
+    split = tile / (tiles_m * tiles_n);
+    tile -= split * tiles_m * tiles_n;
+  }
+  const int64_t kb = split * args.k_per_split;
   const int64_t K = min(args.K, kb + args.k_per_split);
-  T* __restrict__ C = static_cast<T*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
+  T* __restrict__ C = static_cast<T*>(args.C) + split * args.c_split_stride;
   const bool conjA = args.flags & kFlagConjA;
   const bool conjB = args.flags & kFlagConjB;
 
   // Tile order: groups of 8 M-tiles sweep N so neighbouring CTAs share B.
-  const int64_t tiles_m = (M + BM - 1) / BM;
-  const int64_t tiles_n = (N + BN - 1) / BN;
   const int64_t t = tile;
   constexpr int64_t G = 8;
   const int64_t first_m = (t / (G * tiles_n)) * G;

@@ -87,6 +87,53 @@ splitk_reduce(const T* __restrict__ work, int splits, const GemmArgs out) {
   }
 }
 
+// Grouped form: output element idx of the launch belongs to the problem with
+// the last begin <= idx (binary search over the descriptors).
+template <class T>
+__global__ void __launch_bounds__(256)
+splitk_reduce_group(const SplitReduce* __restrict__ probs, int n, int64_t total) {
+  for (int64_t idx = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; idx < total;
+       idx += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (probs[mid].begin <= idx) lo = mid; else hi = mid - 1;
+    }
+    const SplitReduce& pr = probs[lo];
+    const GemmArgs& out = pr.out;
+    const int64_t M = out.M, MN = out.M * out.N;
+    const int64_t e = idx - pr.begin;
+    const T* __restrict__ work = static_cast<const T*>(pr.work);
+    double2 acc = make_double2(0.0, 0.0);
+    for (int s = 0; s < pr.splits; ++s) {
+      const double2 v = widen(work[s * MN + e]);
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+    const int64_t m = e % M, nn = e / M;
+    T* p = static_cast<T*>(out.C) + offs(out.rsC, out.uC_m, m) + offs(out.csC, out.uC_n, nn);
+    double2 r = cmul(make_double2(out.alpha[0], out.alpha[1]), acc);
+    if (out.flags & kFlagAccumulate) {
+      const double2 o = widen(*p);
+      r.x += o.x;
+      r.y += o.y;
+    } else if (!(out.flags & kFlagBetaZero)) {
+      const double2 o = cmul(make_double2(out.beta[0], out.beta[1]), widen(*p));
+      r.x += o.x;
+      r.y += o.y;
+    }
+    narrow(r, p);
+  }
+}
+
+template <class T>
+cudaError_t launch_group(const SplitReduce* dev, int n, int64_t total, cudaStream_t stream) {
+  if (total <= 0 || n <= 0) return cudaSuccess;
+  const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 16);
+  splitk_reduce_group<T><<<static_cast<unsigned>(blocks), 256, 0, stream>>>(dev, n, total);
+  return cudaGetLastError();
+}
+
 template <class T>
 cudaError_t launch(const void* work, int splits, const GemmArgs& out, cudaStream_t stream) {
   const int64_t mn = out.M * out.N;
@@ -106,6 +153,17 @@ cudaError_t launch_splitk_reduce(int dtype, const void* work, int splits, const 
     case 1: return launch<double>(work, splits, out, stream);
     case 2: return launch<float2>(work, splits, out, stream);
     case 3: return launch<double2>(work, splits, out, stream);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_splitk_reduce_group(int dtype, const SplitReduce* dev, int n, int64_t total,
+                                       cudaStream_t stream) {
+  switch (dtype) {
+    case 0: return launch_group<float>(dev, n, total, stream);
+    case 1: return launch_group<double>(dev, n, total, stream);
+    case 2: return launch_group<float2>(dev, n, total, stream);
+    case 3: return launch_group<double2>(dev, n, total, stream);
   }
   return cudaErrorInvalidValue;
 }

@@ -201,6 +201,76 @@ __device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, ui
                : "memory");
 }
 
+// Gather loaders (96 threads, lt = 0..95): one 8-byte cp.async per complex
+// element through the scatter vectors, zero fill outside the tile's valid
+// rows / columns and [k0, ke).  Source addresses are formed eight at a time
+// before their copies are issued, so the index loads of non-uniform bundles
+// overlap instead of each waiting behind the previous cp.async.
+//   A, raw layout [k][m] (512 B rows): element e = lt + 96 i, m = e % 64,
+//      k = e / 64 (consecutive threads walk m: coalesced where M is unit
+//      stride).
+//   B, raw layout [n][k] 128 B-swizzled: thread lt always takes k = lt % 16
+//      (96 is a multiple of 16), so one K offset per stage; n = lt / 16 + 6 i.
+// kBatch addresses are formed per round (8 where registers allow; the
+// persistent kernel's loader warps run on a reduced register budget).
+template <int kBatch>
+__device__ __forceinline__ void gather_a_stage(const GemmArgs& g, uint32_t dst, int lt,
+                                               int64_t m0, int64_t k0, int64_t ke) {
+  const float2* __restrict__ A = static_cast<const float2*>(g.A);
+  constexpr int kPer = (kTileMc * kStepK + kLoaders - 1) / kLoaders;  // 11
+#pragma unroll 1
+  for (int i0 = 0; i0 < kPer; i0 += kBatch) {
+    const float2* src[kBatch];
+    uint32_t okm = 0;
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int e = lt + kLoaders * (i0 + j);
+      const int m = e % kTileMc, k = e / kTileMc;
+      const bool in = (i0 + j < kPer) && e < kTileMc * kStepK && (m0 + m < g.M) && (k0 + k < ke);
+      src[j] = in ? A + offs(g.rsA, g.uA_m, m0 + m) + offs(g.csA, g.uA_k, k0 + k) : A;
+      okm |= in ? (1u << j) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int e = lt + kLoaders * (i0 + j);
+      if (i0 + j < kPer && e < kTileMc * kStepK) {
+        const int m = e % kTileMc, k = e / kTileMc;
+        ptx::cp_async_8(dst + static_cast<uint32_t>(k * 512 + m * 8), src[j],
+                        ((okm >> j) & 1u) ? 8u : 0u);
+      }
+    }
+  }
+}
+
+template <int kBatch>
+__device__ __forceinline__ void gather_b_stage(const GemmArgs& g, uint32_t dst, int lt,
+                                               int64_t n0, int64_t k0, int64_t ke) {
+  const float2* __restrict__ B = static_cast<const float2*>(g.B);
+  const int k = lt & (kStepK - 1);
+  const bool kin = k0 + k < ke;
+  const int64_t rk = kin ? offs(g.rsB, g.uB_k, k0 + k) : 0;
+  constexpr int kStride = kLoaders / kStepK;                     // 6
+  constexpr int kPer = (kTileN + kStride - 1) / kStride;         // 22
+#pragma unroll 1
+  for (int i0 = 0; i0 < kPer; i0 += kBatch) {
+    const float2* src[kBatch];
+    uint32_t okm = 0;
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int n = (lt >> 4) + kStride * (i0 + j);
+      const bool in = kin && (i0 + j < kPer) && n < kTileN && (n0 + n < g.N);
+      src[j] = in ? B + rk + offs(g.csB, g.uB_n, n0 + n) : B;
+      okm |= in ? (1u << j) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int n = (lt >> 4) + kStride * (i0 + j);
+      if (i0 + j < kPer && n < kTileN)
+        ptx::cp_async_8(dst + swz128(n, k), src[j], ((okm >> j) & 1u) ? 8u : 0u);
+    }
+  }
+}
+
 // Position of one output tile in the tile list.
 struct TileRef {
   const TcProblem* p;
@@ -393,8 +463,6 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       const TileRef tr = locate(&single, group, nprob, t);
       const TcProblem* p = tr.p;
       const GemmArgs& g = p->g;
-      const float2* __restrict__ A = static_cast<const float2*>(g.A);
-      const float2* __restrict__ B = static_cast<const float2*>(g.B);
       const int amode = p->amode, bmode = p->bmode;
       // Element offsets of the 16-row A blocks and 16-column B blocks of this
       // tile (block TMA modes), per tile; rows past the edge read row 0's
@@ -495,24 +563,8 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
             continue;
           }
         }
-        if (amode == kAGather) {
-          // [k][m]: consecutive threads walk m (coalesced where M is unit stride).
-          for (int e = lt; e < kTileMc * kStepK; e += kLoaders) {
-            const int m = e % kTileMc, k = e / kTileMc;
-            const bool in = (tr.m0 + m < g.M) && (k0 + k < tr.ke);
-            const float2* src = in ? A + offs(g.rsA, g.uA_m, tr.m0 + m) + offs(g.csA, g.uA_k, k0 + k) : A;
-            ptx::cp_async_8(raw_a(r) + static_cast<uint32_t>(k * 512 + m * 8), src, in ? 8u : 0u);
-          }
-        }
-        if (bmode == kBGather) {
-          // [n][k] swizzled: consecutive threads walk k.
-          for (int e = lt; e < kTileN * kStepK; e += kLoaders) {
-            const int k = e % kStepK, n = e / kStepK;
-            const bool in = (tr.n0 + n < g.N) && (k0 + k < tr.ke);
-            const float2* src = in ? B + offs(g.rsB, g.uB_k, k0 + k) + offs(g.csB, g.uB_n, tr.n0 + n) : B;
-            ptx::cp_async_8(raw_b(r) + swz128(n, k), src, in ? 8u : 0u);
-          }
-        }
+        if (amode == kAGather) gather_a_stage<4>(g, raw_a(r), lt, tr.m0, k0, tr.ke);
+        if (bmode == kBGather) gather_b_stage<4>(g, raw_b(r), lt, tr.n0, k0, tr.ke);
         ptx::cp_async_arrive_noinc(raw_full(r));
       }
       if (stop) break;
@@ -961,8 +1013,6 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   } else if (tid < kConvBase) {
     // ------------------------------------------------------------ loaders ---
     const int lt = tid - kLoaderBase;  // 0..95
-    const float2* __restrict__ A = static_cast<const float2*>(args.A);
-    const float2* __restrict__ B = static_cast<const float2*>(args.B);
     // Gather work of this thread: fixed rows / columns, K walked per stage.
     for (int64_t s = 0; s < ksteps; ++s) {
       const int r = static_cast<int>(s % kRaw);
@@ -986,24 +1036,8 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * n0), static_cast<int>(k0), raw_full(r));
       }
       if (kGather) {
-        if (AMode == kGatherMK) {
-          // [k][m]: consecutive threads walk m (coalesced where M is unit stride).
-          for (int e = lt; e < kTileMc * kStepK; e += kLoaders) {
-            const int m = e % kTileMc, k = e / kTileMc;
-            const bool ok = (m0 + m < M) && (k0 + k < K);
-            const float2* src = ok ? A + offs(args.rsA, args.uA_m, m0 + m) + offs(args.csA, args.uA_k, k0 + k) : A;
-            ptx::cp_async_8(raw_a(r) + static_cast<uint32_t>(k * 512 + m * 8), src, ok ? 8u : 0u);
-          }
-        }
-        if (BMode == kGatherNK) {
-          // [n][k] swizzled: consecutive threads walk k.
-          for (int e = lt; e < kTileN * kStepK; e += kLoaders) {
-            const int k = e % kStepK, n = e / kStepK;
-            const bool ok = (n0 + n < N) && (k0 + k < K);
-            const float2* src = ok ? B + offs(args.rsB, args.uB_k, k0 + k) + offs(args.csB, args.uB_n, n0 + n) : B;
-            ptx::cp_async_8(raw_b(r) + swz128(n, k), src, ok ? 8u : 0u);
-          }
-        }
+        if (AMode == kGatherMK) gather_a_stage<8>(args, raw_a(r), lt, m0, k0, K);
+        if (BMode == kGatherNK) gather_b_stage<8>(args, raw_b(r), lt, n0, k0, K);
         ptx::cp_async_arrive_noinc(raw_full(r));
       }
     }

@@ -59,14 +59,16 @@ def test_sweep_batch_matches_fp64(ctx, torch_cuda, graph, autotune, tmp_path, mo
 
 def test_all_tensor_core_batch_with_dependencies(ctx, torch_cuda):
     """Every item on the tensor cores and two dependency levels: one
-    persistent launch resolves the dependencies in the kernel."""
+    persistent launch resolves the dependencies in the kernel (K of every
+    item within the per-tile cap, so no item is split)."""
     import t1m_gb300 as t1m
     torch = torch_cuda
     rng = np.random.default_rng(32)
     v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
     items, checks = [], []
     for _ in range(5):
-        x, a, y, b, q = (int(val) for val in rng.choice([32, 48, 64, 96], 5))
+        x, a, q = (int(val) for val in rng.choice([32, 48, 64, 96], 3))
+        y, b = (int(val) for val in rng.choice([16, 32], 2))
         X1 = _rand(rng, (x, a), np.complex64, 0.2)
         X2 = _rand(rng, (a, y, b), np.complex64, 0.2)
         X3 = _rand(rng, (y, b, q), np.complex64, 0.2)
@@ -130,3 +132,44 @@ def test_group_rejects_forward_dependency_and_host_data(ctx, torch_cuda):
     w = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
     with pytest.raises(t1m.T1MError):
         t1m.Group([(1.0, w(g[0]), "ab", w(g[1]), "bc", 0.0, w(g[2]), "ac", 1)], ctx=ctx)
+
+
+def test_group_split_k_long_contractions(ctx, torch_cuda):
+    """Items whose K exceeds the per-tile cap are split across CTAs (partials in
+    the group's workspace, one FP64 reduction per dependency level): a
+    tensor-core item, a skinny plain item, their dependents, complex alpha and
+    a nonzero beta applied by the reduction."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    rng = np.random.default_rng(34)
+    v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+    X = _rand(rng, (96, 3000), np.complex64, 0.1)
+    Y = _rand(rng, (3000, 160), np.complex64, 0.1)
+    P = _rand(rng, (200, 5000), np.complex64, 0.1)
+    Q = _rand(rng, (5000, 3), np.complex64, 0.1)
+    Z = _rand(rng, (160, 64), np.complex64, 0.1)
+    W = _rand(rng, (3, 40), np.complex64, 0.1)
+    C0 = _rand(rng, (200, 3), np.complex64, 1.0)
+    g = {k: torch.from_numpy(a.copy()).cuda() for k, a in
+         dict(X=X, Y=Y, P=P, Q=Q, Z=Z, W=W, C0=C0).items()}
+    r1 = torch.zeros((96, 160), dtype=torch.complex64, device="cuda")
+    r2 = g["C0"].clone()
+    o1 = torch.zeros((96, 64), dtype=torch.complex64, device="cuda")
+    o2 = torch.zeros((200, 40), dtype=torch.complex64, device="cuda")
+    al = 0.5 - 0.25j
+    items = [(1.0, v(g["X"]), "xa", v(g["Y"]), "ay", 0.0, v(r1), "xy", -1),
+             (al, v(g["P"]), "xa", v(g["Q"]), "at", 0.5, v(r2), "xt", -1),
+             (1.0, v(r1), "xy", v(g["Z"]), "yq", 0.0, v(o1), "xq", 0),
+             (1.0, v(r2), "xt", v(g["W"]), "tz", 0.0, v(o2), "xz", 1)]
+    grp = t1m.Group(items, ctx=ctx, graph=True)
+    rep = grp.launch()
+    # Two levels, each with main launches and one reduction.
+    assert rep.kernels >= 3
+    d = lambda z: z.astype(np.complex128)  # noqa: E731
+    R1 = d(X) @ d(Y)
+    R2 = al * (d(P) @ d(Q)) + 0.5 * d(C0)
+    for got, want, tol in ((r1, R1, 2e-6), (r2, R2, 4e-6), (o1, R1 @ d(Z), 2e-6),
+                           (o2, R2 @ d(W), 4e-6)):
+        mx, fro = no.rel_errors(got.cpu().numpy(), want)
+        assert mx < tol and fro < tol, (mx, fro, tol)
+    grp.close()
