@@ -584,8 +584,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
 #pragma unroll
       for (int cc = 0; cc < 4; ++cc) {
         uint32_t r[16];
-        ptx::tmem_ld16(tmem + lane_base + col + 64u * wg + 16u * cc, r);
-        ptx::tmem_wait_ld();
+        ptx::tmem_ld16_sync(tmem + lane_base + col + 64u * wg + 16u * cc, r);
 #pragma unroll
         for (int j = 0; j < 16; ++j) master[16 * cc + j] += __uint_as_float(r[j]);
       }
@@ -865,8 +864,22 @@ struct TmaMaps {
 // kind::f16 MMAs per product, A pieces packed two per TMEM column (16 columns
 // each) and B pieces in 64-byte halves of the 128-byte swizzled rows (pieces
 // 0 | 1 in the first B buffer, piece 2 in the second).
+// Converter warpgroups of the one-tile kernel.  Two (8 warps, 384 threads in
+// all, 64 accumulator columns per converter thread) measured faster on GB300
+// than four (16 warps, 640 threads, 32 columns each: 180 vs 198 TFLOP/s at
+// complex64 4096^3, 3xTF32), whose 96-register budget and doubled per-stage
+// barrier traffic outweigh the extra warps to interleave.
+constexpr int kCW1 = 2;
+constexpr int kConverters1 = 128 * kCW1;
+constexpr int kThreads1 = kConvBase + kConverters1;
+constexpr int kAK1 = kStepK / kCW1;                          // complex k of A per thread
+constexpr int kMC1 = kTileN / kCW1;                          // accumulator columns per thread
+constexpr int kBP1 = (kTileN * kStepK / 2) / kConverters1;   // 16-byte B pieces per thread
+constexpr int kB16P1 = (kTileN * kStepK / 4) / kConverters1; // bf16 B chunks per thread
+static_assert(kAK1 % 4 == 0 && kMC1 % 16 == 0 && kBP1 >= 1 && kB16P1 >= 1, "converter split");
+
 template <int AMode, int BMode, int Prec>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreads1, 1)
 tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
   constexpr bool kBF16 = Prec != kPrecTF32x3;
   constexpr int kPieces = Prec == kPrecBF16x6 ? 3 : 2;
@@ -907,15 +920,15 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   if (tid == 32) {
     for (int r = 0; r < kRaw; ++r) {
       ptx::mbar_init(raw_full(r), kRawArrivals);
-      ptx::mbar_init(raw_empty(r), kConverters / 32);
+      ptx::mbar_init(raw_empty(r), kConverters1 / 32);
     }
     for (int s = 0; s < kStages; ++s) {
-      ptx::mbar_init(full_bar(s), kConverters / 32);
+      ptx::mbar_init(full_bar(s), kConverters1 / 32);
       ptx::mbar_init(empty_bar(s), 1);
     }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(chunk_full(b), 1);
-      ptx::mbar_init(chunk_empty(b), kConverters / 32);
+      ptx::mbar_init(chunk_empty(b), kConverters1 / 32);
     }
     ptx::mbar_init(acc_bar, 1);
     ptx::fence_mbar_init();
@@ -1043,8 +1056,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     }
   } else {
     // -------------------------------------------- converters, fold, epilogue ---
+    // kCW1 warpgroups: warpgroup wg converts complex k [kAK1 wg, kAK1 (wg + 1))
+    // of every staged A row and a 1/kCW1 share of the B tile, and folds and
+    // writes accumulator columns [kMC1 wg, kMC1 (wg + 1)) of its TMEM lanes.
     const int pt = tid - kConvBase;
-    const int wg = pt >> 7;          // which half of the K-step (A) / of N (B, C)
+    const int wg = pt >> 7;
     const int q = (pt >> 5) & 3;     // TMEM lane quarter of this warp
     const int rho = 32 * q + lane;   // real row = TMEM lane
     const int ci = rho >> 1;         // complex row in the tile
@@ -1054,18 +1070,17 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     const bool conjB = args.flags & kFlagConjB;
     const bool row_ok = (m0 + ci) < M;
 
-    float master[64];
+    float master[kMC1];
 #pragma unroll
-    for (int j = 0; j < 64; ++j) master[j] = 0.f;
+    for (int j = 0; j < kMC1; ++j) master[j] = 0.f;
 
     // Fold chunk accumulator at column `col` into the FP32 master registers
-    // (round-to-nearest adds): this thread's lane, 64 columns.
+    // (round-to-nearest adds): this thread's lane, kMC1 columns.
     auto fold_from = [&](uint32_t col) {
 #pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
+      for (int cc = 0; cc < kMC1 / 16; ++cc) {
         uint32_t r[16];
-        ptx::tmem_ld16(tmem + lane_base + col + 64u * wg + 16u * cc, r);
-        ptx::tmem_wait_ld();
+        ptx::tmem_ld16_sync(tmem + lane_base + col + kMC1 * wg + 16u * cc, r);
 #pragma unroll
         for (int j = 0; j < 16; ++j) master[16 * cc + j] += __uint_as_float(r[j]);
       }
@@ -1073,15 +1088,17 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
 
     // Loop-invariant shared-memory offsets of this thread's raw reads and
     // operand writes.
-    uint32_t aoff[8];
+    uint32_t aoff[kAK1];
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-      aoff[j] = (AMode == kTmaKM) ? swz128(ci, 8 * wg + 2 * (j >> 1))
-                                  : static_cast<uint32_t>((8 * wg + j) * 512 + ci * 8);
-    uint32_t bsrc[4], boff[4][2];
+    for (int j = 0; j < kAK1; ++j)
+      aoff[j] = (AMode == kTmaKM) ? swz128(ci, kAK1 * wg + 2 * (j >> 1))
+                                  : static_cast<uint32_t>((kAK1 * wg + j) * 512 + ci * 8);
+    // TF32 B: piece j of this thread (id = pt + kConverters1 j) is two complex
+    // k of one column ([n][k] tiles) or one k of two columns ([k][n] tile).
+    uint32_t bsrc[kBP1], boff[kBP1][2];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int id = pt + 256 * j;
+    for (int j = 0; j < kBP1; ++j) {
+      const int id = pt + kConverters1 * j;
       if (BMode == kTmaKN) {
         const int k = id >> 6, n = 2 * (id & 63);
         bsrc[j] = static_cast<uint32_t>(k * 1024 + n * 8);
@@ -1094,20 +1111,22 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         boff[j][1] = 0;
       }
     }
-    // bf16 B: id = pt + 256 j covers column n = id & 127 and complex k
-    // 4 kq .. 4 kq + 3 (kq = id >> 7): two 16-byte raw reads (one per k pair)
-    // in the swizzled [n][k] tiles, four 8-byte reads in the [k][n] tile;
-    // one 16-byte chunk (8 bf16) per piece, chunk kq (+4 for odd pieces) of
-    // row n.  Consecutive lanes take consecutive n: no bank conflicts.
-    uint32_t b16src[2], b16row[2], b16chunk[2];
+    // bf16 B: id = pt + kConverters1 j covers column n = id & 127 and complex
+    // k 4 kq .. 4 kq + 3 (kq = id >> 7): two 16-byte raw reads (one per k
+    // pair) in the swizzled [n][k] tiles, four 8-byte reads in the [k][n]
+    // tile; one 16-byte chunk (8 bf16) per piece, chunk kq (+4 for odd
+    // pieces) of row n.  Consecutive lanes take consecutive n: no bank
+    // conflicts.
+    uint32_t b16src[kB16P1], b16row[kB16P1], b16chunk[kB16P1];
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int id = pt + 256 * j;
+    for (int j = 0; j < kB16P1; ++j) {
+      const int id = pt + kConverters1 * j;
       const int n = id & 127, kq = id >> 7;
       b16src[j] = (BMode == kTmaKN) ? static_cast<uint32_t>(4 * kq * 1024 + n * 8) : swz128(n, 4 * kq);
       b16row[j] = static_cast<uint32_t>((n >> 3) * 1024 + (n & 7) * 128);
       b16chunk[j] = static_cast<uint32_t>(kq ^ (n & 7));
     }
+    constexpr int kBV = kBP1 > 2 * kB16P1 ? kBP1 : 2 * kB16P1;
 
     bool ok = true;
     int r = 0, st = 0;
@@ -1118,28 +1137,28 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         ok = false;
         break;
       }
-      // A: eight complex k (this half of the step) of complex row ci.
+      // A: kAK1 complex k (this warpgroup's share of the step) of row ci.
       const uint32_t ra = raw_a(r), rb = raw_b(r);
-      float2 av[8];
+      float2 av[kAK1];
       if (AMode == kTmaKM) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < kAK1 / 2; ++j) {
           const float4 v = lds128(ra + aoff[2 * j]);
           av[2 * j] = make_float2(v.x, v.y);
           av[2 * j + 1] = make_float2(v.z, v.w);
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < 8; ++j) av[j] = lds64(ra + aoff[j]);
+        for (int j = 0; j < kAK1; ++j) av[j] = lds64(ra + aoff[j]);
       }
-      // B: four 16-byte pieces (two complex each) of the raw tile.
-      float4 bv[4];
+      // B: this thread's 16-byte pieces (two complex each) of the raw tile.
+      float4 bv[kBV];
       if constexpr (!kBF16) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bv[j] = lds128(rb + bsrc[j]);
+        for (int j = 0; j < kBP1; ++j) bv[j] = lds128(rb + bsrc[j]);
       } else {
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
+        for (int j = 0; j < kB16P1; ++j) {
           if (BMode == kTmaKN) {
             const float2 t0 = lds64(rb + b16src[j]), t1 = lds64(rb + b16src[j] + 1024u);
             const float2 t2 = lds64(rb + b16src[j] + 2048u), t3 = lds64(rb + b16src[j] + 3072u);
@@ -1163,12 +1182,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       ptx::tc_fence_after();
       const uint32_t ob = op0 + st * kOpBytes;
       if constexpr (kBF16) {
-        // A -> TMEM: the 1M row pairs of this thread's 8 complex k, split
-        // into kPieces bf16x2 words each; piece p at columns +16p (+8 for
-        // the second half of the K-step).
-        uint32_t w[3][8];
+        // A -> TMEM: the 1M row pairs of this thread's kAK1 complex k, split
+        // into kPieces bf16x2 words each; piece p at columns +16p.
+        uint32_t w[3][kAK1];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < kAK1; ++j) {
           float2 v = av[j];
           if (conjA) v.y = -v.y;
           if (!row_ok) v = make_float2(0.f, 0.f);
@@ -1176,12 +1194,12 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           const float x1 = part ? v.x : -v.y;
           split_bf16<kPieces>(x0, x1, w[0][j], w[1][j], w[2][j]);
         }
-        const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 8u * wg;
+        const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + kAK1 * wg;
 #pragma unroll
-        for (int p = 0; p < kPieces; ++p) ptx::tmem_st8(a_col + 16u * p, w[p]);
+        for (int p = 0; p < kPieces; ++p) ptx::tmem_st_n<kAK1>(a_col + 16u * p, w[p]);
         // B -> shared memory: 4 complex k of column n, re/im interleaved.
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
+        for (int j = 0; j < kB16P1; ++j) {
           float4 v0 = bv[2 * j], v1 = bv[2 * j + 1];
           if (conjB) {
             v0.y = -v0.y;
@@ -1189,21 +1207,21 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
             v1.y = -v1.y;
             v1.w = -v1.w;
           }
-          uint32_t q[4][3];
-          split_bf16<kPieces>(v0.x, v0.y, q[0][0], q[0][1], q[0][2]);
-          split_bf16<kPieces>(v0.z, v0.w, q[1][0], q[1][1], q[1][2]);
-          split_bf16<kPieces>(v1.x, v1.y, q[2][0], q[2][1], q[2][2]);
-          split_bf16<kPieces>(v1.z, v1.w, q[3][0], q[3][1], q[3][2]);
+          uint32_t qw[4][3];
+          split_bf16<kPieces>(v0.x, v0.y, qw[0][0], qw[0][1], qw[0][2]);
+          split_bf16<kPieces>(v0.z, v0.w, qw[1][0], qw[1][1], qw[1][2]);
+          split_bf16<kPieces>(v1.x, v1.y, qw[2][0], qw[2][1], qw[2][2]);
+          split_bf16<kPieces>(v1.z, v1.w, qw[3][0], qw[3][1], qw[3][2]);
 #pragma unroll
           for (int p = 0; p < kPieces; ++p)
             sts128(ob + (p >> 1) * kBHalfBytes + b16row[j] + ((b16chunk[j] ^ (4u * (p & 1))) << 4),
-                   q[0][p], q[1][p], q[2][p], q[3][p]);
+                   qw[0][p], qw[1][p], qw[2][p], qw[3][p]);
         }
       } else {
         // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
-        uint32_t hi[16], lo[16];
+        uint32_t hi[2 * kAK1], lo[2 * kAK1];
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
+        for (int j = 0; j < kAK1; ++j) {
           float2 v = av[j];
           if (conjA) v.y = -v.y;
           if (!row_ok) v = make_float2(0.f, 0.f);
@@ -1215,12 +1233,12 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           hi[2 * j + 1] = s1.hi;
           lo[2 * j + 1] = s1.lo;
         }
-        const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 16u * wg;
-        ptx::tmem_st16(a_col, hi);
-        ptx::tmem_st16(a_col + 32u, lo);
+        const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 2 * kAK1 * wg;
+        ptx::tmem_st_n<2 * kAK1>(a_col, hi);
+        ptx::tmem_st_n<2 * kAK1>(a_col + 32u, lo);
         // B -> shared memory (swizzled K-major hi and lo tiles).
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < kBP1; ++j) {
           float4 v = bv[j];
           if (conjB) {
             v.y = -v.y;
@@ -1289,11 +1307,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
       const int64_t rowC = row_ok ? offs(args.rsC, args.uC_m, m0 + ci) : 0;
 #pragma unroll
-      for (int j = 0; j < 32; ++j) {
+      for (int j = 0; j < kMC1 / 2; ++j) {
         const float v0 = master[2 * j], v1 = master[2 * j + 1];
         const float send = part ? v0 : v1;
         const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-        const int col = wg * 64 + 2 * j + part;
+        const int col = wg * kMC1 + 2 * j + part;
         const float re = part ? recv : v0;
         const float im = part ? v1 : recv;
         const int64_t n = n0 + col;
@@ -1322,7 +1340,6 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     ptx::tmem_dealloc(tmem, kTmemCols);
   }
 }
-
 
 // ------------------------------------------------------------------ host ---
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -1388,7 +1405,7 @@ cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  tc1m_contract<AMode, BMode, Prec><<<tiles, kThreads, kSmemBytes, stream>>>(args, maps, err_flag);
+  tc1m_contract<AMode, BMode, Prec><<<tiles, kThreads1, kSmemBytes, stream>>>(args, maps, err_flag);
   return cudaGetLastError();
 }
 
