@@ -60,7 +60,7 @@ def _peaks() -> dict:
 def _profiled_traffic():
     """DRAM bytes (read + write) per launch of the tensor-core kernel on this
     workload, from the committed ncu summary (None if absent)."""
-    p = ROOT / "profiles" / "tc3xtf32_ijkl_klmn_64.md"
+    p = ROOT / "profiles" / "tc1m_contract_ijkl_klmn_64.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -375,7 +375,7 @@ def run_gpu(args) -> None:
                          "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",
                          "frac": kernel_tflops / peak,
                          "traffic": _profiled_traffic() if tc_method == "tc_3xtf32" else None,
-                         "traffic_source": "profiles/tc3xtf32_ijkl_klmn_64.md (ncu dram bytes "
+                         "traffic_source": "profiles/tc1m_contract_ijkl_klmn_64.md (ncu dram bytes "
                                            "read+write per launch)",
                          "peak_note": peak_note},
             "e2e": {"value": world * FLOPS / e2e_s / 1e12, "unit": "TFLOP/s",
