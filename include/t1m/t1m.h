@@ -185,4 +185,31 @@ void contract_scaled(const T alpha, const tensor<T, ndim_a>& a, const std::strin
   detail::run(ctx, alpha, a, labels_a, b, labels_b, beta, c, labels_c, 0u);
 }
 
+/// Adjoint of C = A*B (no reference counterpart): dA = dC * conj(B) and
+/// dB = conj(A) * dC in the conjugate-Wirtinger convention (for real T, plain
+/// transposed products).  dA / dB are overwritten; either may be null.
+/// Forwards to t1m_contract_vjp.
+template <TensorScalar T, std::size_t ndim_a, std::size_t ndim_b, std::size_t ndim_c>
+void contract_vjp(const tensor<T, ndim_c>& dc, const std::string& labels_c,
+                  const tensor<T, ndim_a>& a, const std::string& labels_a,
+                  const tensor<T, ndim_b>& b, const std::string& labels_b,
+                  tensor<T, ndim_a>* da, tensor<T, ndim_b>* db,
+                  context* ctx = default_context()) {
+  detail::view<T, ndim_c> vdc(dc);
+  detail::view<T, ndim_a> va(a);
+  detail::view<T, ndim_b> vb(b);
+  if (da) {
+    detail::view<T, ndim_a> vda(*da);
+    ctx->check(t1m_contract_vjp(ctx->handle(), detail::dtype_of<T>(), &vdc.t, labels_c.c_str(),
+                                &va.t, labels_a.c_str(), &vb.t, labels_b.c_str(), &vda.t, nullptr,
+                                0u, nullptr));
+  }
+  if (db) {
+    detail::view<T, ndim_b> vdb(*db);
+    ctx->check(t1m_contract_vjp(ctx->handle(), detail::dtype_of<T>(), &vdc.t, labels_c.c_str(),
+                                &va.t, labels_a.c_str(), &vb.t, labels_b.c_str(), nullptr, &vdb.t,
+                                0u, nullptr));
+  }
+}
+
 }  // namespace t1m

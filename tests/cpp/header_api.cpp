@@ -97,6 +97,29 @@ int main() {
     }
   expect(zerr < 1e-12, "complex<double> contract_scaled");
 
+  // Adjoint of C = A*B: dA[i,k] = sum_j dC[i,j] conj(B[k,j]),
+  // dB[k,j] = sum_i conj(A[i,k]) dC[i,j].
+  std::vector<std::complex<double>> DC(6 * 8), DA(6 * 7), DB(7 * 8);
+  for (auto& x : DC) x = {rnd<double>(seed), rnd<double>(seed)};
+  t1m::tensor<std::complex<double>, 2> dc({6, 8}, DC.data());
+  t1m::tensor<std::complex<double>, 2> da({6, 7}, DA.data());
+  t1m::tensor<std::complex<double>, 2> db({7, 8}, DB.data());
+  t1m::contract_vjp(dc, "ij", za, "ik", zb, "kj", &da, &db);
+  double verr = 0;
+  for (int i = 0; i < 6; ++i)
+    for (int k = 0; k < 7; ++k) {
+      std::complex<double> s = 0;
+      for (int j = 0; j < 8; ++j) s += DC[i + 6 * j] * std::conj(ZB[k + 7 * j]);
+      verr = std::max(verr, std::abs(s - DA[i + 6 * k]));
+    }
+  for (int k = 0; k < 7; ++k)
+    for (int j = 0; j < 8; ++j) {
+      std::complex<double> s = 0;
+      for (int i = 0; i < 6; ++i) s += std::conj(ZA[i + 6 * k]) * DC[i + 6 * j];
+      verr = std::max(verr, std::abs(s - DB[k + 7 * j]));
+    }
+  expect(verr < 1e-12, "complex<double> contract_vjp (dA, dB)");
+
   std::printf("%s\n", fails ? "header api FAILED" : "header api ok");
   return fails ? 1 : 0;
 }
