@@ -558,7 +558,7 @@ def workload_batch(args):
         items.append((1.0, v(R), "xsyb", v(X3), "ytb", 0.0, v(O), "xst", i1))
         keep.append((X1, X2, X3, R, O))
         flops += 8.0 * x * y * s * b * a + 8.0 * x * s * t * y * b
-    grp = t1m.Group(items, ctx=ctx, graph=True, autotune=True)
+    grp = t1m.Group(items, ctx=ctx, graph=True, autotune=not args.no_autotune)
     grouped_ms = _events_ms(torch, lambda: grp.launch(timed=False), args.steps, args.warmup)
     # Sampled check of a few items against FP64.
     errs = []
@@ -641,6 +641,8 @@ def main() -> None:
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "config2", "logmag", "batch", "vjp"])
     ap.add_argument("--items", type=int, default=1024)
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch workload: heuristic kernel families instead of the autotuner")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

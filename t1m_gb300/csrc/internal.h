@@ -75,6 +75,12 @@ constexpr uint32_t kFlagAccumulate = 1u;  // C += alpha*AB (beta ignored)
 constexpr uint32_t kFlagConjA = 2u;
 constexpr uint32_t kFlagConjB = 4u;
 constexpr uint32_t kFlagBetaZero = 16u;  // BLAS semantics with beta == 0
+// Epilogue store forms of the tensor-core kernels (set by tc_prepare):
+// C columns pairwise contiguous and every pair 16-byte aligned (one 16-byte
+// store per two complex values), and C column offsets unit stride inside
+// every 16-column block (one offset lookup per 16 columns).
+constexpr uint32_t kFlagCPairs = 32u;
+constexpr uint32_t kFlagCCol16 = 64u;
 
 // Launchers.  Return cudaError_t of the launch.
 // simt.cu: plain FP32/FP64 kernel; `splits` CTA rows along K.

@@ -216,7 +216,12 @@ __device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, ui
 template <int kBatch>
 __device__ __forceinline__ void gather_a_stage(const GemmArgs& g, uint32_t dst, int lt,
                                                int64_t m0, int64_t k0, int64_t ke) {
+  // Descriptor fields in registers: the cp.async statements clobber memory,
+  // which would otherwise force a reload of every field per element.
   const float2* __restrict__ A = static_cast<const float2*>(g.A);
+  const int64_t* __restrict__ rsA = g.rsA;
+  const int64_t* __restrict__ csA = g.csA;
+  const int64_t uA_m = g.uA_m, uA_k = g.uA_k, M = g.M;
   constexpr int kPer = (kTileMc * kStepK + kLoaders - 1) / kLoaders;  // 11
 #pragma unroll 1
   for (int i0 = 0; i0 < kPer; i0 += kBatch) {
@@ -226,8 +231,8 @@ __device__ __forceinline__ void gather_a_stage(const GemmArgs& g, uint32_t dst, 
     for (int j = 0; j < kBatch; ++j) {
       const int e = lt + kLoaders * (i0 + j);
       const int m = e % kTileMc, k = e / kTileMc;
-      const bool in = (i0 + j < kPer) && e < kTileMc * kStepK && (m0 + m < g.M) && (k0 + k < ke);
-      src[j] = in ? A + offs(g.rsA, g.uA_m, m0 + m) + offs(g.csA, g.uA_k, k0 + k) : A;
+      const bool in = (i0 + j < kPer) && e < kTileMc * kStepK && (m0 + m < M) && (k0 + k < ke);
+      src[j] = in ? A + offs(rsA, uA_m, m0 + m) + offs(csA, uA_k, k0 + k) : A;
       okm |= in ? (1u << j) : 0u;
     }
 #pragma unroll
@@ -246,6 +251,8 @@ template <int kBatch>
 __device__ __forceinline__ void gather_b_stage(const GemmArgs& g, uint32_t dst, int lt,
                                                int64_t n0, int64_t k0, int64_t ke) {
   const float2* __restrict__ B = static_cast<const float2*>(g.B);
+  const int64_t* __restrict__ csB = g.csB;
+  const int64_t uB_n = g.uB_n, N = g.N;
   const int k = lt & (kStepK - 1);
   const bool kin = k0 + k < ke;
   const int64_t rk = kin ? offs(g.rsB, g.uB_k, k0 + k) : 0;
@@ -258,8 +265,8 @@ __device__ __forceinline__ void gather_b_stage(const GemmArgs& g, uint32_t dst, 
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const int n = (lt >> 4) + kStride * (i0 + j);
-      const bool in = kin && (i0 + j < kPer) && n < kTileN && (n0 + n < g.N);
-      src[j] = in ? B + rk + offs(g.csB, g.uB_n, n0 + n) : B;
+      const bool in = kin && (i0 + j < kPer) && n < kTileN && (n0 + n < N);
+      src[j] = in ? B + rk + offs(csB, uB_n, n0 + n) : B;
       okm |= in ? (1u << j) : 0u;
     }
 #pragma unroll
@@ -267,6 +274,88 @@ __device__ __forceinline__ void gather_b_stage(const GemmArgs& g, uint32_t dst, 
       const int n = (lt >> 4) + kStride * (i0 + j);
       if (i0 + j < kPer && n < kTileN)
         ptx::cp_async_8(dst + swz128(n, k), src[j], ((okm >> j) & 1u) ? 8u : 0u);
+    }
+  }
+}
+
+// Epilogue of one converter thread: accumulator columns [col0, col0 + kCols)
+// of real row 2 ci + part (part 0 holds the real parts of complex row ci,
+// part 1 the imaginary parts).  Lane pairs swap halves with two shuffles per
+// four columns so that each thread holds complete complex values: part 0
+// writes columns 4q, 4q + 1 and part 1 columns 4q + 2, 4q + 3 of every group
+// of four.  With kFlagCPairs the two values go out as one 16-byte access (a
+// lane pair fills a 32-byte sector); with kFlagCCol16 one column offset is
+// looked up per 16 columns.  C <- alpha*acc (+ beta*C, or + C when
+// accumulating).
+template <int kCols>
+__device__ __forceinline__ void store_tile(const GemmArgs& g, float2* __restrict__ Cp,
+                                           int64_t row, bool row_ok, int64_t n0, int col0,
+                                           int part, const float (&master)[kCols]) {
+  const uint32_t flags = g.flags;
+  const bool accumulate = flags & kFlagAccumulate;
+  const bool beta_zero = flags & kFlagBetaZero;
+  const bool pairs = flags & kFlagCPairs;
+  const bool col16 = flags & kFlagCCol16;
+  const float ar = (float)g.alpha[0], ai = (float)g.alpha[1];
+  const float br = (float)g.beta[0], bi = (float)g.beta[1];
+  const int64_t N = g.N;
+  const int64_t* __restrict__ csC = g.csC;
+  const int64_t uC_n = g.uC_n;
+  const int64_t rowC = row_ok ? offs(g.rsC, g.uC_m, row) : 0;
+  float2* __restrict__ Cr = Cp + rowC;
+  int64_t blk = 0;  // offset of the current 16-column block (kFlagCCol16)
+#pragma unroll
+  for (int q = 0; q < kCols / 4; ++q) {
+    const float s0 = part ? master[4 * q] : master[4 * q + 2];
+    const float s1 = part ? master[4 * q + 1] : master[4 * q + 3];
+    const float r0 = __shfl_xor_sync(0xffffffffu, s0, 1);
+    const float r1 = __shfl_xor_sync(0xffffffffu, s1, 1);
+    const float re0 = part ? r0 : master[4 * q], im0 = part ? master[4 * q + 2] : r0;
+    const float re1 = part ? r1 : master[4 * q + 1], im1 = part ? master[4 * q + 3] : r1;
+    const int c = col0 + 4 * q + 2 * part;
+    const int64_t n = n0 + c;
+    if (col16 && (q & 3) == 0) {
+      const int64_t nb = n0 + col0 + 16 * (q >> 2);
+      blk = (row_ok && nb < N) ? offs(csC, uC_n, nb) : 0;
+    }
+    if (!row_ok || n >= N) continue;
+    const int64_t on = col16 ? blk + (c - col0 - 16 * (q >> 2)) : offs(csC, uC_n, n);
+    const bool second = n + 1 < N;
+    const float t0r = ar * re0 - ai * im0, t0i = ar * im0 + ai * re0;
+    const float t1r = ar * re1 - ai * im1, t1i = ar * im1 + ai * re1;
+    if (pairs && second) {
+      float4* p4 = reinterpret_cast<float4*>(Cr + on);
+      if (accumulate) {
+        const float4 o = *p4;
+        *p4 = make_float4(o.x + t0r, o.y + t0i, o.z + t1r, o.w + t1i);
+      } else if (beta_zero) {
+        *p4 = make_float4(t0r, t0i, t1r, t1i);
+      } else {
+        const float4 o = *p4;
+        *p4 = make_float4(t0r + (br * o.x - bi * o.y), t0i + (br * o.y + bi * o.x),
+                          t1r + (br * o.z - bi * o.w), t1i + (br * o.w + bi * o.z));
+      }
+    } else {
+      float2* p0 = Cr + on;
+      float2* p1 = second ? Cr + (col16 ? on + 1 : offs(csC, uC_n, n + 1)) : p0;
+      if (accumulate) {
+        const float2 o = *p0;
+        *p0 = make_float2(o.x + t0r, o.y + t0i);
+        if (second) {
+          const float2 o1 = *p1;
+          *p1 = make_float2(o1.x + t1r, o1.y + t1i);
+        }
+      } else if (beta_zero) {
+        *p0 = make_float2(t0r, t0i);
+        if (second) *p1 = make_float2(t1r, t1i);
+      } else {
+        const float2 o = *p0;
+        *p0 = make_float2(t0r + (br * o.x - bi * o.y), t0i + (br * o.y + bi * o.x));
+        if (second) {
+          const float2 o1 = *p1;
+          *p1 = make_float2(t1r + (br * o1.x - bi * o1.y), t1i + (br * o1.y + bi * o1.x));
+        }
+      }
     }
   }
 }
@@ -563,8 +652,8 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
             continue;
           }
         }
-        if (amode == kAGather) gather_a_stage<4>(g, raw_a(r), lt, tr.m0, k0, tr.ke);
-        if (bmode == kBGather) gather_b_stage<4>(g, raw_b(r), lt, tr.n0, k0, tr.ke);
+        if (amode == kAGather) gather_a_stage<2>(g, raw_a(r), lt, tr.m0, k0, tr.ke);
+        if (bmode == kBGather) gather_b_stage<2>(g, raw_b(r), lt, tr.n0, k0, tr.ke);
         ptx::cp_async_arrive_noinc(raw_full(r));
       }
       if (stop) break;
@@ -794,37 +883,9 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       }
       chunk_cnt = c_last + 1;
 
-      const bool accumulate = g.flags & kFlagAccumulate;
-      const bool beta_zero = g.flags & kFlagBetaZero;
-      const float ar = (float)g.alpha[0], ai = (float)g.alpha[1];
-      const float br = (float)g.beta[0], bi = (float)g.beta[1];
       const int64_t split = tr.kb / g.k_per_split;
       float2* __restrict__ Cp = static_cast<float2*>(g.C) + split * g.c_split_stride;
-      const int64_t rowC = row_ok ? offs(g.rsC, g.uC_m, tr.m0 + ci) : 0;
-#pragma unroll
-      for (int j = 0; j < 32; ++j) {
-        const float v0 = master[2 * j], v1 = master[2 * j + 1];
-        const float send = part ? v0 : v1;
-        const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-        const int col = wg * 64 + 2 * j + part;
-        const float re = part ? recv : v0;
-        const float im = part ? v1 : recv;
-        const int64_t n = tr.n0 + col;
-        if (row_ok && n < g.N) {
-          float2* pc = Cp + rowC + offs(g.csC, g.uC_n, n);
-          const float tr_ = ar * re - ai * im;
-          const float ti_ = ar * im + ai * re;
-          if (accumulate) {
-            const float2 o = *pc;
-            *pc = make_float2(o.x + tr_, o.y + ti_);
-          } else if (beta_zero) {
-            *pc = make_float2(tr_, ti_);
-          } else {
-            const float2 o = *pc;
-            *pc = make_float2(tr_ + (br * o.x - bi * o.y), ti_ + (br * o.y + bi * o.x));
-          }
-        }
-      }
+      store_tile<64>(g, Cp, tr.m0 + ci, row_ok, tr.n0, wg * 64, part, master);
       if (done) {
         // Publish the tile: every converter's stores, then one release-add.
         converters_sync();
@@ -1299,37 +1360,9 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       const int64_t c_last = (ksteps - 1) / kFold;
       fold_from((c_last & 1) ? kChunkCol1 : kChunkCol0);
       fold_from(kCorrCol);
-      const bool accumulate = args.flags & kFlagAccumulate;
-      const bool beta_zero = args.flags & kFlagBetaZero;
-      const float ar = (float)args.alpha[0], ai = (float)args.alpha[1];
-      const float br = (float)args.beta[0], bi = (float)args.beta[1];
       float2* __restrict__ Cp =
           static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
-      const int64_t rowC = row_ok ? offs(args.rsC, args.uC_m, m0 + ci) : 0;
-#pragma unroll
-      for (int j = 0; j < kMC1 / 2; ++j) {
-        const float v0 = master[2 * j], v1 = master[2 * j + 1];
-        const float send = part ? v0 : v1;
-        const float recv = __shfl_xor_sync(0xffffffffu, send, 1);
-        const int col = wg * kMC1 + 2 * j + part;
-        const float re = part ? recv : v0;
-        const float im = part ? v1 : recv;
-        const int64_t n = n0 + col;
-        if (row_ok && n < N) {
-          float2* p = Cp + rowC + offs(args.csC, args.uC_n, n);
-          const float tr = ar * re - ai * im;
-          const float ti = ar * im + ai * re;
-          if (accumulate) {
-            const float2 o = *p;
-            *p = make_float2(o.x + tr, o.y + ti);
-          } else if (beta_zero) {
-            *p = make_float2(tr, ti);
-          } else {
-            const float2 o = *p;
-            *p = make_float2(tr + (br * o.x - bi * o.y), ti + (br * o.y + bi * o.x));
-          }
-        }
-      }
+      store_tile<kMC1>(args, Cp, m0 + ci, row_ok, n0, wg * kMC1, part, master);
     }
   }
 
@@ -1456,6 +1489,45 @@ bool common_block_stride16(const std::vector<int64_t>& rows, const std::vector<i
   return true;
 }
 
+// Epilogue store flags of a problem (kFlagCPairs, kFlagCCol16) from C's row
+// and column offsets: the uniform strides where the arguments carry them (a
+// uniform bundle, the dense split-K workspace), else the plan's vectors.
+uint32_t c_store_flags(const GemmArgs& g, const HostPlan& plan) {
+  auto col = [&](int64_t n) { return g.uC_n >= 0 ? n * g.uC_n : plan.csC[n]; };
+  auto row = [&](int64_t m) { return g.uC_m >= 0 ? m * g.uC_m : plan.rsC[m]; };
+  uint32_t f = 0;
+  bool col16 = true;
+  if (g.uC_n >= 0) {
+    col16 = g.uC_n == 1 || g.N <= 1;
+  } else {
+    for (int64_t b = 0; b < g.N && col16; b += 16)
+      for (int64_t i = b + 1; i < std::min<int64_t>(g.N, b + 16); ++i)
+        if (col(i) != col(b) + (i - b)) {
+          col16 = false;
+          break;
+        }
+  }
+  if (col16) f |= kFlagCCol16;
+  bool pairs = reinterpret_cast<uintptr_t>(g.C) % 16 == 0;
+  if (pairs) {
+    if (g.uC_m >= 0) {
+      pairs = g.uC_m % 2 == 0 || g.M <= 1;
+    } else {
+      for (int64_t m = 0; m < g.M && pairs; ++m) pairs = row(m) % 2 == 0;
+    }
+  }
+  if (pairs) {
+    if (g.uC_n >= 0) {
+      pairs = g.uC_n == 1;
+    } else {
+      for (int64_t n = 0; n + 1 < g.N && pairs; n += 2)
+        pairs = col(n) % 2 == 0 && col(n + 1) == col(n) + 1;
+    }
+  }
+  if (pairs) f |= kFlagCPairs;
+  return f;
+}
+
 std::mutex g_attr_mutex;
 bool g_attr_set = false;
 
@@ -1477,6 +1549,7 @@ bool tc_supported(int method, int dtype, const HostPlan& plan) {
 bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p) {
   std::memset(static_cast<void*>(p), 0, sizeof(*p));
   p->g = g;
+  p->g.flags = (g.flags & ~(kFlagCPairs | kFlagCCol16)) | c_store_flags(g, plan);
   p->tiles_m = static_cast<int32_t>((g.M + kTileMc - 1) / kTileMc);
   p->tiles_n = static_cast<int32_t>((g.N + kTileN - 1) / kTileN);
   p->splits = splits;
@@ -1606,12 +1679,12 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                    : (b_uniform && p.bmode == kBKN) ? kTmaKN : kGatherNK;
     switch (method) {
       case T1M_METHOD_TC_BF16X3:
-        e = launch_a<kPrecBF16x3>(am, bm, args, maps, stream, err_flag, grid);
+        e = launch_a<kPrecBF16x3>(am, bm, p.g, maps, stream, err_flag, grid);
         break;
       case T1M_METHOD_TC_BF16X6:
-        e = launch_a<kPrecBF16x6>(am, bm, args, maps, stream, err_flag, grid);
+        e = launch_a<kPrecBF16x6>(am, bm, p.g, maps, stream, err_flag, grid);
         break;
-      default: e = launch_a<kPrecTF32x3>(am, bm, args, maps, stream, err_flag, grid); break;
+      default: e = launch_a<kPrecTF32x3>(am, bm, p.g, maps, stream, err_flag, grid); break;
     }
   } else {
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
