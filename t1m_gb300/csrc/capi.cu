@@ -722,7 +722,7 @@ struct TuneCache {
     cudaGetDeviceProperties(&prop, device);
     int drv = 0;
     cudaDriverGetVersion(&drv);
-    header = std::string("t1m_gb300-tune v1 ") + prop.name + " sms=" +
+    header = std::string("t1m_gb300-tune v2 ") + prop.name + " sms=" +
              std::to_string(prop.multiProcessorCount) + " driver=" + std::to_string(drv);
     for (char& ch : header)
       if (ch == '\n') ch = ' ';
@@ -787,6 +787,7 @@ struct t1m_group {
     int64_t offset;   // first descriptor in tc_dev / simt_dev
     int count;
     int64_t tiles;
+    int nmax = 16;    // skinny launches: column bound of the kernel (4 or 16)
   };
   std::vector<std::vector<Launch>> levels;
   bool single_tc = false;
@@ -820,8 +821,12 @@ int enqueue_group(t1m_group* g, cudaStream_t s) {
           e = launch_splitk_reduce_group(g->dtype,
                                          static_cast<const SplitReduce*>(g->reduce_dev) + l.offset,
                                          l.count, l.tiles, s);
+        else if (l.family == kFamSimtSkinny)
+          e = launch_skinny_group(g->dtype, l.nmax,
+                                  static_cast<const SimtProblem*>(g->simt_dev) + l.offset, l.count,
+                                  l.tiles, s);
         else
-          e = launch_simt_group(g->dtype, l.family == kFamSimtSkinny,
+          e = launch_simt_group(g->dtype, false,
                                 static_cast<const SimtProblem*>(g->simt_dev) + l.offset, l.count,
                                 l.tiles, s);
         ++kernels;
@@ -962,10 +967,13 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
       const std::string key = shape_class(dtype, hp);
       auto it = g_tune.choice.find(key);
       if (it != g_tune.choice.end()) {
-        family[i] = it->second;
+        // A shape class spans N up to twice its bucket: the skinny kernel
+        // only takes outputs of at most kSkinnyMaxN columns.
+        if (it->second != kFamSimtSkinny || hp.N <= kSkinnyMaxN) family[i] = it->second;
         continue;
       }
-      std::vector<int> cands = {kFamSimt, kFamSimtSkinny};
+      std::vector<int> cands = {kFamSimt};
+      if (hp.N <= kSkinnyMaxN) cands.push_back(kFamSimtSkinny);
       if (dtype == T1M_COMPLEX64 && ctx->method != T1M_METHOD_PLAIN) cands.push_back(kFamTC);
       // Each candidate runs with its own split count (the main kernel only:
       // the reduction is the same for all of them) into a scratch output.
@@ -1002,14 +1010,20 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
             le = ok ? tc_launch_persistent(&tp, nullptr, 1, tc_problem_tiles(tp), ctx->num_sms,
                                            nullptr, ctx->stream, ctx->d_err)
                     : cudaErrorInvalidValue;
+          } else if (f == kFamSimtSkinny) {
+            SimtProblem sp{probe, 0};
+            cudaMemcpy(pd, &sp, sizeof(sp), cudaMemcpyHostToDevice);
+            const int nmax = hp.N <= 4 ? 4 : 16;
+            le = launch_skinny_group(dtype, nmax, static_cast<SimtProblem*>(pd), 1,
+                                     skinny_tiles(probe, nsp, nmax), ctx->stream);
           } else {
             SimtProblem sp{probe, 0};
             cudaMemcpy(pd, &sp, sizeof(sp), cudaMemcpyHostToDevice);
             int bm, bn;
-            simt_group_tile(dtype, f == kFamSimtSkinny, &bm, &bn);
+            simt_group_tile(dtype, false, &bm, &bn);
             const int64_t tiles = nsp * ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
-            le = launch_simt_group(dtype, f == kFamSimtSkinny, static_cast<SimtProblem*>(pd), 1,
-                                   tiles, ctx->stream);
+            le = launch_simt_group(dtype, false, static_cast<SimtProblem*>(pd), 1, tiles,
+                                   ctx->stream);
           }
           cudaEventRecord(ctx->ev[5], ctx->stream);
           if (le != cudaSuccess || cudaEventSynchronize(ctx->ev[5]) != cudaSuccess) {
@@ -1081,6 +1095,13 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
   for (int lv = 0; lv <= max_level; ++lv) {
     for (int fam : {kFamTC, kFamSimt, kFamSimtSkinny}) {
       t1m_group::Launch L{fam, fam == kFamTC ? int64_t(tcs.size()) : int64_t(simts.size()), 0, 0};
+      if (fam == kFamSimtSkinny) {
+        // One kernel instance per launch: the smallest column bound that
+        // covers every item of the launch.
+        L.nmax = 4;
+        for (int i = 0; i < n; ++i)
+          if (level[i] == lv && family[i] == fam && plans[i].N > 4) L.nmax = 16;
+      }
       for (int i = 0; i < n; ++i) {
         if (level[i] != lv || family[i] != fam) continue;
         const HostPlan& hp = plans[i];
@@ -1102,9 +1123,13 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
           L.tiles += t;
           g->tc_total += t;
           tcs.push_back(tp);
+        } else if (fam == kFamSimtSkinny) {
+          SimtProblem sp{main_args[i], L.tiles};
+          L.tiles += skinny_tiles(main_args[i], splits[i], L.nmax);
+          simts.push_back(sp);
         } else {
           int bm, bn;
-          simt_group_tile(dtype, fam == kFamSimtSkinny, &bm, &bn);
+          simt_group_tile(dtype, false, &bm, &bn);
           SimtProblem sp{main_args[i], L.tiles};
           L.tiles += splits[i] * ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
           simts.push_back(sp);

@@ -103,6 +103,18 @@ void simt_group_tile(int dtype, bool skinny, int* bm, int* bn);
 cudaError_t launch_simt_group(int dtype, bool skinny, const SimtProblem* dev, int nprob,
                               int64_t total_tiles, cudaStream_t stream);
 
+// Skinny grouped launches (simt.cu): outputs of at most `nmax` (4 or 16)
+// columns, bound by reading A once.  Rows per CTA: one warp per row (16 / nmax
+// rows per warp, 8 warps) when A has unit K stride, else one thread per row.
+constexpr int kSkinnyMaxN = 16;
+__host__ __device__ constexpr int skinny_rows(bool k_unit, int nmax) {
+  return k_unit ? 8 * (16 / nmax) : 256;
+}
+// Tiles of one skinny problem: splits x ceil(M / rows).
+int64_t skinny_tiles(const GemmArgs& g, int splits, int nmax);
+cudaError_t launch_skinny_group(int dtype, int nmax, const SimtProblem* dev, int nprob,
+                                int64_t total_tiles, cudaStream_t stream);
+
 // splitk.cu: C <- alpha * sum_s W[s] + beta*C (or C + alpha*sum) with the sum
 // in FP64.  W holds `splits` dense M x N partials, m fastest, of the dtype.
 cudaError_t launch_splitk_reduce(int dtype, const void* work, int splits, const GemmArgs& out,

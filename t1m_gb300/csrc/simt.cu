@@ -294,7 +294,186 @@ cudaError_t launch_group(const SimtProblem* dev, int nprob, int64_t total_tiles,
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------- skinny ---
+// Outputs of at most NMAX columns (the second step of a sweep update,
+// xsyb,ytb->xst with t <= 4, or any GEMV-like contraction): the work streams A
+// once, so instead of a square tile a CTA takes a block of rows and one K
+// chunk.  The chunk's B (all N columns, zero-padded to NMAX) is staged in
+// shared memory, transposed so lanes read consecutive k; A rows are read along
+// their unit-stride direction:
+//   K unit stride: one warp per row (16 / NMAX rows per warp), lanes over k
+//     (256-byte coalesced reads), lane partial sums reduced across the warp;
+//   otherwise: one thread per row, k in order (coalesced across threads where
+//     M is unit stride), the chunk's K offsets staged in shared memory.
+// Tiles are numbered split-major per problem; a split writes its partial
+// product to its workspace slice exactly like the other kernels.
+__device__ __forceinline__ float shfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ float2 shfl_xor(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+__device__ __forceinline__ double2 shfl_xor(double2 v, int m) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+
+template <class T>
+__device__ __forceinline__ void skinny_store(const GemmArgs& g, T* C, int64_t m, int64_t n, T v) {
+  T* p = C + offs(g.rsC, g.uC_m, m) + offs(g.csC, g.uC_n, n);
+  const T ab = mul(scal<T>(g.alpha), v);
+  if (g.flags & kFlagAccumulate)
+    *p = add(*p, ab);
+  else if (g.flags & kFlagBetaZero)
+    *p = ab;
+  else
+    *p = add(ab, mul(scal<T>(g.beta), *p));
+}
+
+template <class T, int NMAX, bool KUNIT>
+__device__ __forceinline__ void skinny_body(const GemmArgs& g, int64_t tile, T (*Bs)[2048 / NMAX],
+                                            int64_t* ks) {
+  constexpr int KB = 2048 / NMAX;            // k per shared-memory chunk
+  constexpr int RW = KUNIT ? 16 / NMAX : 1;  // rows per warp (K unit) / per thread
+  constexpr int BMr = skinny_rows(KUNIT, NMAX);
+  const int64_t M = g.M, N = g.N, K = g.K;
+  const int64_t tiles_m = (M + BMr - 1) / BMr;
+  const int64_t split = tile / tiles_m;
+  const int64_t m0 = (tile - split * tiles_m) * BMr;
+  const int64_t kb = split * g.k_per_split;
+  const int64_t ke = min(K, kb + g.k_per_split);
+  T* __restrict__ C = static_cast<T*>(g.C) + split * g.c_split_stride;
+  const T* __restrict__ A = static_cast<const T*>(g.A);
+  const T* __restrict__ B = static_cast<const T*>(g.B);
+  const bool conjA = g.flags & kFlagConjA;
+  const bool conjB = g.flags & kFlagConjB;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // Rows of this thread (K unit: this warp's rows; otherwise: one row).
+  int64_t rowoff[RW];
+  bool rowok[RW];
+#pragma unroll
+  for (int r = 0; r < RW; ++r) {
+    const int64_t m = KUNIT ? m0 + warp * RW + r : m0 + tid;
+    rowok[r] = m < M;
+    rowoff[r] = rowok[r] ? offs(g.rsA, g.uA_m, m) : 0;
+  }
+  T acc[RW][NMAX];
+#pragma unroll
+  for (int r = 0; r < RW; ++r)
+#pragma unroll
+    for (int n = 0; n < NMAX; ++n) acc[r][n] = zero<T>();
+
+  for (int64_t k0 = kb; k0 < ke; k0 += KB) {
+    const int kn = static_cast<int>(min(static_cast<int64_t>(KB), ke - k0));
+    __syncthreads();  // the previous chunk is consumed
+    for (int e = tid; e < KB * NMAX; e += kThreads) {
+      const int n = e / KB, kk = e % KB;
+      T v = zero<T>();
+      if (n < N && kk < kn)
+        v = conj_if(B[offs(g.rsB, g.uB_k, k0 + kk) + offs(g.csB, g.uB_n, n)], conjB);
+      Bs[n][kk] = v;
+    }
+    if (!KUNIT)
+      for (int kk = tid; kk < kn; kk += kThreads) ks[kk] = offs(g.csA, g.uA_k, k0 + kk);
+    __syncthreads();
+    if (KUNIT) {
+#pragma unroll 4
+      for (int kk = lane; kk < kn; kk += 32) {
+#pragma unroll
+        for (int r = 0; r < RW; ++r) {
+          if (!rowok[r]) continue;
+          const T a = conj_if(A[rowoff[r] + k0 + kk], conjA);
+#pragma unroll
+          for (int n = 0; n < NMAX; ++n) mac(acc[r][n], a, Bs[n][kk]);
+        }
+      }
+    } else if (rowok[0]) {
+#pragma unroll 4
+      for (int kk = 0; kk < kn; ++kk) {
+        const T a = conj_if(A[rowoff[0] + ks[kk]], conjA);
+#pragma unroll
+        for (int n = 0; n < NMAX; ++n) mac(acc[0][n], a, Bs[n][kk]);
+      }
+    }
+  }
+
+  if (KUNIT) {
+#pragma unroll
+    for (int r = 0; r < RW; ++r) {
+#pragma unroll
+      for (int n = 0; n < NMAX; ++n) {
+        T v = acc[r][n];
+#pragma unroll
+        for (int d = 16; d >= 1; d >>= 1) v = add(v, shfl_xor(v, d));
+        acc[r][n] = v;
+      }
+      const int64_t m = m0 + warp * RW + r;
+      if (lane == 0 && rowok[r])
+#pragma unroll
+        for (int n = 0; n < NMAX; ++n)
+          if (n < N) skinny_store(g, C, m, n, acc[r][n]);
+    }
+  } else if (rowok[0]) {
+#pragma unroll
+    for (int n = 0; n < NMAX; ++n)
+      if (n < N) skinny_store(g, C, m0 + tid, n, acc[0][n]);
+  }
+}
+
+template <class T, int NMAX>
+__global__ void __launch_bounds__(kThreads)
+skinny_contract(const SimtProblem* group, int nprob) {
+  __shared__ GemmArgs ga;
+  __shared__ __align__(16) T Bs[NMAX][2048 / NMAX];
+  __shared__ int64_t ks[2048 / NMAX];
+  int64_t tile = blockIdx.x;
+  int lo = 0, hi = nprob - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (group[mid].tile_begin <= tile) lo = mid; else hi = mid - 1;
+  }
+  tile -= group[lo].tile_begin;
+  if (threadIdx.x == 0) ga = group[lo].g;
+  __syncthreads();
+  if (ga.uA_k == 1)
+    skinny_body<T, NMAX, true>(ga, tile, Bs, ks);
+  else
+    skinny_body<T, NMAX, false>(ga, tile, Bs, ks);
+}
+
+template <class T, int NMAX>
+cudaError_t launch_skinny(const SimtProblem* dev, int nprob, int64_t total_tiles,
+                          cudaStream_t stream) {
+  if (total_tiles <= 0) return cudaSuccess;
+  if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  skinny_contract<T, NMAX><<<static_cast<unsigned>(total_tiles), kThreads, 0, stream>>>(dev,
+                                                                                       nprob);
+  return cudaGetLastError();
+}
+
+template <int NMAX>
+cudaError_t launch_skinny_dtype(int dtype, const SimtProblem* dev, int nprob, int64_t tiles,
+                                cudaStream_t stream) {
+  switch (dtype) {
+    case 0: return launch_skinny<float, NMAX>(dev, nprob, tiles, stream);
+    case 1: return launch_skinny<double, NMAX>(dev, nprob, tiles, stream);
+    case 2: return launch_skinny<float2, NMAX>(dev, nprob, tiles, stream);
+    case 3: return launch_skinny<double2, NMAX>(dev, nprob, tiles, stream);
+  }
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace
+
+int64_t skinny_tiles(const GemmArgs& g, int splits, int nmax) {
+  const int64_t rows = skinny_rows(g.uA_k == 1, nmax);
+  return int64_t(splits) * ((g.M + rows - 1) / rows);
+}
+
+cudaError_t launch_skinny_group(int dtype, int nmax, const SimtProblem* dev, int nprob,
+                                int64_t total_tiles, cudaStream_t stream) {
+  return nmax <= 4 ? launch_skinny_dtype<4>(dtype, dev, nprob, total_tiles, stream)
+                   : launch_skinny_dtype<16>(dtype, dev, nprob, total_tiles, stream);
+}
 
 void simt_group_tile(int dtype, bool skinny, int* bm, int* bn) {
   if (skinny) {

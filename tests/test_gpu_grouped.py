@@ -173,3 +173,44 @@ def test_group_split_k_long_contractions(ctx, torch_cuda):
         mx, fro = no.rel_errors(got.cpu().numpy(), want)
         assert mx < tol and fro < tol, (mx, fro, tol)
     grp.close()
+
+
+@pytest.mark.parametrize("dt", [np.complex64, np.float64])
+def test_group_skinny_outputs(ctx, torch_cuda, dt):
+    """Grouped items with at most 16 output columns run on the skinny kernel:
+    A with unit K stride (one warp per row) and with unit M stride (one
+    thread per row), N = 3 and N = 13 (the 4- and 16-column instances), a
+    long K that is split, alpha and beta applied through the reduction."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    rng = np.random.default_rng(35)
+
+    def r(shape):
+        x = rng.uniform(-1, 1, shape)
+        if np.dtype(dt).kind == "c":
+            x = x + 1j * rng.uniform(-1, 1, shape)
+        return x.astype(dt)
+
+    # C-ordered arrays, handed over as col-major views with reversed extents
+    # and labels: the last label of each string is the unit-stride mode.
+    cases = [("ak", "kn", "an", dict(a=300, k=5000, n=3)),    # K unit stride
+             ("ka", "kn", "an", dict(a=700, k=2100, n=13)),   # M unit stride
+             ("ak", "kn", "an", dict(a=37, k=64, n=13))]      # short K, ragged rows
+    items, checks = [], []
+    v = lambda z: t1m.tensor(list(z.shape)[::-1], z, t1m.col_major)  # noqa: E731
+    alpha = 0.5 - 0.25j if np.dtype(dt).kind == "c" else 0.5
+    for la, lb, lc, ext in cases:
+        A, B = r([ext[c] for c in la]), r([ext[c] for c in lb])
+        C0 = r([ext[c] for c in lc])
+        ga, gb, gc = (torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in (A, B, C0))
+        items.append((alpha, v(ga), la[::-1], v(gb), lb[::-1], 0.25, v(gc), lc[::-1], -1))
+        ref = alpha * np.einsum(f"{la},{lb}->{lc}", A.astype(np.complex128),
+                                B.astype(np.complex128)) + 0.25 * C0.astype(np.complex128)
+        checks.append((gc, ref, (ga, gb)))
+    grp = t1m.Group(items, ctx=ctx, graph=True)
+    grp.launch()
+    tol = 2e-6 if np.dtype(dt) == np.complex64 else 1e-12
+    for gc, ref, _ in checks:
+        mx, fro = no.rel_errors(gc.cpu().numpy().astype(np.complex128), ref)
+        assert mx < tol and fro < tol, (mx, fro)
+    grp.close()
