@@ -375,23 +375,42 @@ __device__ __forceinline__ void skinny_body(const GemmArgs& g, int64_t tile, T (
     if (!KUNIT)
       for (int kk = tid; kk < kn; kk += kThreads) ks[kk] = offs(g.csA, g.uA_k, k0 + kk);
     __syncthreads();
+    // kU k-steps of every row are loaded before any of them is used, so
+    // each thread keeps kU x RW loads in flight (the kernel is bound by the
+    // latency of streaming A).
+    constexpr int kU = 4;
     if (KUNIT) {
-#pragma unroll 4
-      for (int kk = lane; kk < kn; kk += 32) {
+      for (int kk0 = lane; kk0 < kn; kk0 += 32 * kU) {
+        T a[kU][RW];
 #pragma unroll
-        for (int r = 0; r < RW; ++r) {
-          if (!rowok[r]) continue;
-          const T a = conj_if(A[rowoff[r] + k0 + kk], conjA);
+        for (int u = 0; u < kU; ++u)
 #pragma unroll
-          for (int n = 0; n < NMAX; ++n) mac(acc[r][n], a, Bs[n][kk]);
+          for (int r = 0; r < RW; ++r) {
+            const int kk = kk0 + 32 * u;
+            a[u][r] = (rowok[r] && kk < kn) ? conj_if(A[rowoff[r] + k0 + kk], conjA) : zero<T>();
+          }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          const int kk = kk0 + 32 * u;
+          if (kk >= kn) break;
+#pragma unroll
+          for (int r = 0; r < RW; ++r)
+#pragma unroll
+            for (int n = 0; n < NMAX; ++n) mac(acc[r][n], a[u][r], Bs[n][kk]);
         }
       }
     } else if (rowok[0]) {
-#pragma unroll 4
-      for (int kk = 0; kk < kn; ++kk) {
-        const T a = conj_if(A[rowoff[0] + ks[kk]], conjA);
+      for (int kk0 = 0; kk0 < kn; kk0 += kU) {
+        T a[kU];
 #pragma unroll
-        for (int n = 0; n < NMAX; ++n) mac(acc[0][n], a, Bs[n][kk]);
+        for (int u = 0; u < kU; ++u)
+          a[u] = kk0 + u < kn ? conj_if(A[rowoff[0] + ks[kk0 + u]], conjA) : zero<T>();
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+          if (kk0 + u >= kn) break;
+#pragma unroll
+          for (int n = 0; n < NMAX; ++n) mac(acc[0][n], a[u], Bs[n][kk0 + u]);
+        }
       }
     }
   }
