@@ -495,7 +495,7 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
   }
   if (!devC && bytesC) {
     if (int st = ensure_stage(ctx, 2, bytesC)) return st;
-    if (readC || hp.spanC != hp.M * hp.N) {
+    if (readC || hp.spanC != hp.M * hp.N * hp.batch) {
       // C's gaps (strided C) must survive the copy back, so it is read too.
       if ((e = cudaMemcpyAsync(ctx->stage[2], c->data, bytesC, cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return cuda_fail(ctx, e, "copy C to device");
@@ -508,13 +508,23 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
   int kernels = 0;
   int used_method = method;
   int splits = 1;
-  if (hp.M > 0 && hp.N > 0) {
+  // Batch labels: one product per batch index, operands shifted by the
+  // index's offsets (the loop runs once without batch labels).
+  const GemmArgs g_all = g;
+  for (int64_t bi = 0; bi < hp.batch && hp.M > 0 && hp.N > 0; ++bi) {
+    int64_t oa, ob, oc;
+    batch_offsets(hp, bi, &oa, &ob, &oc);
+    g = g_all;
+    g.A = static_cast<const char*>(g_all.A) + oa * static_cast<int64_t>(es);
+    g.B = static_cast<const char*>(g_all.B) + ob * static_cast<int64_t>(es);
+    g.C = static_cast<char*>(g_all.C) + oc * static_cast<int64_t>(es);
     g.k_per_split = std::max<int64_t>(hp.K, 1);
     g.c_split_stride = 0;
+    int nk = 0;
     if (hp.K == 0) {
       // C <- beta*C (or unchanged): nothing to multiply; handled by the plain
       // kernel with an empty K loop.
-      e = launch_simt(dtype, g, 1, s, &kernels);
+      e = launch_simt(dtype, g, 1, s, &nk);
       used_method = T1M_METHOD_PLAIN;
     } else {
       const bool dmma_ok =
@@ -544,19 +554,20 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
         gm.c_split_stride = hp.M * hp.N;
       }
       if (method == T1M_METHOD_PLAIN) {
-        e = launch_simt(dtype, gm, splits, s, &kernels);
+        e = launch_simt(dtype, gm, splits, s, &nk);
       } else if (method == T1M_METHOD_DMMA) {
-        e = launch_dmma(dtype, gm, splits, s, &kernels);
+        e = launch_dmma(dtype, gm, splits, s, &nk);
       } else {
         std::string err;
-        e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &kernels, &err);
+        e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err);
         if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
       }
       if (e == cudaSuccess && splits > 1) {
         e = launch_splitk_reduce(dtype, ctx->work, splits, g, s);
-        ++kernels;
+        ++nk;
       }
     }
+    kernels += nk;
     if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
   }
   if (timing) cudaEventRecord(ctx->ev[2], s);
@@ -579,7 +590,8 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     report->m = hp.M;
     report->n = hp.N;
     report->k = hp.K;
-    report->flops = (cplx ? 8.0 : 2.0) * double(hp.M) * double(hp.N) * double(hp.K);
+    report->flops =
+        (cplx ? 8.0 : 2.0) * double(hp.M) * double(hp.N) * double(hp.K) * double(hp.batch);
     report->h2d_bytes = h2d;
     report->d2h_bytes = d2h;
     report->kernels = kernels;
@@ -895,6 +907,10 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
                         it.labels_c, &plans[i], &err);
     if (st != T1M_OK) return fail(ctx, st, "group item " + std::to_string(i) + ": " + err);
     const HostPlan& hp = plans[i];
+    if (!hp.modes_b.empty())
+      return fail(ctx, T1M_ERR_LABELS, "group item " + std::to_string(i) +
+                                           ": batch labels (in A, B and C) are taken by "
+                                           "t1m_contract, not by grouped launches");
     if (hp.M > 0 && hp.N > 0 && hp.K > 0 &&
         (!is_device_pointer(it.a->data) || !is_device_pointer(it.b->data) ||
          !is_device_pointer(it.c->data)))

@@ -26,10 +26,20 @@ struct Mode {
 // Element (m, n) of the matricised problem lives at
 //   A: rsA[m] + csA[k]   B: rsB[k] + csB[n]   C: rsC[m] + csC[n]
 // (the reference's rscat/cscat vectors, t1m.h:141-174, in element units).
+// A batch (Hadamard) mode: a label of A, B and C alike.  The contraction is
+// one independent product per batch index (no reference counterpart: the
+// reference leaves such labels undefined).
+struct BatchMode {
+  int64_t extent, sa, sb, sc;
+  char label;
+};
+
 struct HostPlan {
   int dtype = 0;
   int64_t M = 0, N = 0, K = 0;
   std::vector<Mode> modes_m, modes_n, modes_k;
+  std::vector<BatchMode> modes_b;  // first mode fastest
+  int64_t batch = 1;               // product of the batch extents
   std::vector<int64_t> rsA, csA, rsB, csB, rsC, csC;
   // Uniform stride of each scatter vector, or -1 when it is not an arithmetic
   // progression (the block-scatter "constant stride" of t1m.h:179-205 taken
@@ -38,6 +48,20 @@ struct HostPlan {
   // Number of elements each tensor spans in memory (1 + sum (e-1)*s).
   int64_t spanA = 0, spanB = 0, spanC = 0;
 };
+
+// Element offsets of batch index `bi` (mixed radix over modes_b, first mode
+// fastest) in A, B and C.
+inline void batch_offsets(const HostPlan& hp, int64_t bi, int64_t* oa, int64_t* ob,
+                          int64_t* oc) {
+  *oa = *ob = *oc = 0;
+  for (const BatchMode& m : hp.modes_b) {
+    const int64_t i = bi % m.extent;
+    bi /= m.extent;
+    *oa += i * m.sa;
+    *ob += i * m.sb;
+    *oc += i * m.sc;
+  }
+}
 
 // Validate labels/extents/strides and build the plan.  Returns a t1m_status
 // and fills *err with a message on failure.

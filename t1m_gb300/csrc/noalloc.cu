@@ -156,6 +156,9 @@ extern "C" int t1m_contract_noalloc(void* stream_ptr, int method, int dtype, con
   int st = build_plan(dtype, a->ndim, a->extents, sa, la, b->ndim, b->extents, sb, lb, c->ndim,
                       c->extents, sc, lc, &hp, &msg);
   if (st != T1M_OK) return finish(err, err_len, st, msg);
+  if (!hp.modes_b.empty())
+    return finish(err, err_len, T1M_ERR_LABELS,
+                  "batch labels (in A, B and C) are taken by t1m_contract only");
   if (hp.M == 0 || hp.N == 0) return finish(err, err_len, T1M_OK, "");
   if (!on_device(c->data) || (hp.K > 0 && (!on_device(a->data) || !on_device(b->data))))
     return finish(err, err_len, T1M_ERR_INVALID_ARGUMENT,

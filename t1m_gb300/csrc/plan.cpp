@@ -117,6 +117,8 @@ int build_plan(int dtype, int na, const int64_t* ea, const int64_t* sa,
   plan->modes_m.clear();
   plan->modes_n.clear();
   plan->modes_k.clear();
+  plan->modes_b.clear();
+  plan->batch = 1;
   // Walk labels in sorted order, as the reference's set operations do.
   for (int ch = 0; ch < 128; ++ch) {
     const Info& x = info[ch];
@@ -124,9 +126,14 @@ int build_plan(int dtype, int na, const int64_t* ea, const int64_t* sa,
     if (!inA && !inB && !inC) continue;
     if (inA && inB) {
       if (inC) {
-        *err = std::string("label '") + static_cast<char>(ch) +
-               "' appears in A, B and C (batch modes are not supported)";
-        return T1M_ERR_LABELS;
+        // Batch (Hadamard) label: one independent product per index.
+        if (ea[x.pa] != eb[x.pb] || ea[x.pa] != ec[x.pc]) {
+          *err = std::string("extent mismatch for batch label '") + static_cast<char>(ch) + "'";
+          return T1M_ERR_LABELS;
+        }
+        plan->modes_b.push_back({ea[x.pa], sa[x.pa], sb[x.pb], sc[x.pc], static_cast<char>(ch)});
+        plan->batch *= ea[x.pa];
+        continue;
       }
       if (ea[x.pa] != eb[x.pb]) {
         *err = std::string("extent mismatch for contracted label '") + static_cast<char>(ch) + "'";

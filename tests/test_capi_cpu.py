@@ -63,6 +63,7 @@ def _t(dims, dt=np.complex64):
     ("ijkl", "klmn", "ijmn", (64,) * 4, (64,) * 4, (64,) * 4, (4096, 4096, 4096)),
     ("ab", "cd", "abcd", (3, 4), (5, 6), (3, 4, 5, 6), (12, 30, 1)),   # outer product
     ("ab", "ab", "", (3, 4), (3, 4), (), (1, 1, 12)),                   # full contraction
+    ("abc", "bc", "ac", (2, 3, 4), (3, 4), (2, 4), (2, 1, 3)),          # batch label c
 ])
 def test_analyze_sizes(built_lib, la, lb, lc, da, db, dc, mnk):
     import t1m_gb300 as t1m
@@ -74,7 +75,7 @@ def test_analyze_sizes(built_lib, la, lb, lc, da, db, dc, mnk):
     ("abb", "bd", "ad", (2, 3, 3), (3, 4), (2, 4), "repeated"),
     ("abc", "bd", "acd", (2, 3, 4), (5, 4), (2, 4, 4), "extent mismatch"),
     ("abc", "cd", "ad", (2, 3, 4), (4, 5), (2, 5), "missing from C"),
-    ("abc", "bc", "ac", (2, 3, 4), (3, 4), (2, 4), "A, B and C"),
+    ("abc", "bc", "ac", (2, 3, 4), (3, 5), (2, 4), "batch label"),
     ("ab", "bc", "acz", (2, 3), (3, 4), (2, 4, 5), "neither A nor B"),
     ("ab", "bc", "a", (2, 3), (3, 4), (2,), "missing from C"),
     ("a#", "bc", "ac", (2, 3), (3, 4), (2, 4), "invalid label"),

@@ -305,8 +305,10 @@ def test_errors_are_reported_not_crashing(ctx):
     import t1m_gb300 as t1m
     A = np.zeros((2, 3), np.complex64)
     with pytest.raises(t1m.T1MError) as e:
-        t1m.contract_scaled(1.0, t1m.tensor.from_array(A), "ab", t1m.tensor.from_array(A),
-                            "ab", 0.0, t1m.tensor.from_array(A), "ab", ctx=ctx)
+        # label d of C appears in neither A nor B
+        t1m.contract_scaled(1.0, t1m.tensor.from_array(A), "ab", t1m.tensor.from_array(A.T.copy()),
+                            "bc", 0.0, t1m.tensor.from_array(np.zeros((2, 2), np.complex64)),
+                            "ad", ctx=ctx)
     assert e.value.status == 2
     # The context stays usable.
     B = np.ones((3, 2), np.complex64)
