@@ -63,6 +63,11 @@ struct t1m_context {
   size_t work_bytes = 0;
   int split_k = 0;
   int num_sms = 152;
+  // Host-operand pipeline: copy-in and copy-out streams beside the compute
+  // stream, ordering events (see run_pipelined).
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  static constexpr int kPipeEvents = 2 + 2 * 8 + 1;
+  cudaEvent_t pev[kPipeEvents] = {};
 };
 
 namespace {
@@ -201,8 +206,8 @@ constexpr size_t kMaxWorkBytes = size_t(2) << 30;
 // has too few tiles, each split keeping at least four K-steps; forced by
 // t1m_set_split_k.  Returns the split count and its K length (a multiple of
 // the kernel's K-step).
-int choose_splits(const t1m_context* ctx, int method, int dtype, const HostPlan& hp,
-                  size_t elem, int64_t* k_per_split) {
+int choose_splits(const t1m_context* ctx, int method, int dtype, int64_t M, int64_t N,
+                  int64_t K, size_t elem, int64_t* k_per_split) {
   int bm, bn, bk, per_sm;
   if (method == T1M_METHOD_PLAIN) {
     simt_tile(dtype, &bm, &bn, &bk);
@@ -214,8 +219,8 @@ int choose_splits(const t1m_context* ctx, int method, int dtype, const HostPlan&
     tc_tile(&bm, &bn, &bk);
     per_sm = 1;
   }
-  const int64_t tiles = ((hp.M + bm - 1) / bm) * ((hp.N + bn - 1) / bn);
-  const int64_t ksteps = (hp.K + bk - 1) / bk;
+  const int64_t tiles = ((M + bm - 1) / bm) * ((N + bn - 1) / bn);
+  const int64_t ksteps = (K + bk - 1) / bk;
   int64_t s = 1;
   if (ctx->split_k > 0) {
     s = ctx->split_k;
@@ -225,7 +230,7 @@ int choose_splits(const t1m_context* ctx, int method, int dtype, const HostPlan&
       s = std::min<int64_t>((target + tiles - 1) / tiles, ksteps / 4);
   }
   s = std::max<int64_t>(1, std::min<int64_t>({s, ksteps, 4096}));
-  while (s > 1 && size_t(s) * size_t(hp.M) * size_t(hp.N) * elem > kMaxWorkBytes) --s;
+  while (s > 1 && size_t(s) * size_t(M) * size_t(N) * elem > kMaxWorkBytes) --s;
   const int64_t steps_per = (ksteps + s - 1) / s;
   *k_per_split = steps_per * bk;
   return static_cast<int>((ksteps + steps_per - 1) / steps_per);
@@ -243,6 +248,244 @@ int ensure_work(t1m_context* ctx, size_t bytes) {
   if (e != cudaSuccess)
     return fail(ctx, T1M_ERR_ALLOC, std::string("split-K workspace: ") + cudaGetErrorString(e));
   ctx->work_bytes = bytes;
+  return T1M_OK;
+}
+
+// One product C = alpha*A*B (+ beta*C) on stream s, its operands already in
+// g (shifted for a batch index or a slab): method checks, split-K (raw
+// partials in the workspace, FP64 reduction with the epilogue) and the
+// kernel launch.  Adds the kernels it launched to *kernels.
+int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
+                   const GemmArgs& g, cudaStream_t s, int* kernels, int* used_method,
+                   int* splits_out) {
+  int nk = 0;
+  int splits = 1;
+  cudaError_t e = cudaSuccess;
+  if (g.K == 0) {
+    // C <- beta*C (or unchanged): nothing to multiply; handled by the plain
+    // kernel with an empty K loop.
+    e = launch_simt(dtype, g, 1, s, &nk);
+    *used_method = T1M_METHOD_PLAIN;
+  } else {
+    const bool dmma_ok =
+        method == T1M_METHOD_DMMA && (dtype == T1M_FLOAT64 || dtype == T1M_COMPLEX128);
+    if (method != T1M_METHOD_PLAIN && !dmma_ok && !tc_supported(method, dtype, hp))
+      return fail(ctx, T1M_ERR_UNSUPPORTED,
+                  std::string("method ") + std::to_string(method) +
+                      " is not available for this dtype/contraction");
+    int64_t kps = g.K;
+    splits = choose_splits(ctx, method, dtype, g.M, g.N, g.K, es, &kps);
+    // Split-K: the main kernel writes raw partial products (alpha = 1,
+    // beta = 0) into dense workspace slices, m fastest; the reduction sums
+    // them in FP64 and applies the epilogue.
+    GemmArgs gm = g;
+    if (splits > 1) {
+      if (int st = ensure_work(ctx, size_t(splits) * size_t(g.M) * size_t(g.N) * es)) return st;
+      gm.C = ctx->work;
+      gm.rsC = nullptr;
+      gm.csC = nullptr;
+      gm.uC_m = 1;
+      gm.uC_n = g.M;
+      gm.alpha[0] = 1.0;
+      gm.alpha[1] = 0.0;
+      gm.beta[0] = gm.beta[1] = 0.0;
+      gm.flags = (g.flags & (kFlagConjA | kFlagConjB)) | kFlagBetaZero;
+      gm.k_per_split = kps;
+      gm.c_split_stride = g.M * g.N;
+    }
+    if (method == T1M_METHOD_PLAIN) {
+      e = launch_simt(dtype, gm, splits, s, &nk);
+    } else if (method == T1M_METHOD_DMMA) {
+      e = launch_dmma(dtype, gm, splits, s, &nk);
+    } else {
+      std::string err;
+      e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err);
+      if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
+    }
+    if (e == cudaSuccess && splits > 1) {
+      e = launch_splitk_reduce(dtype, ctx->work, splits, g, s);
+      ++nk;
+    }
+  }
+  *kernels += nk;
+  *splits_out = splits;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
+  return T1M_OK;
+}
+
+// Host operands: the contraction is cut into slabs along N (B and C
+// streamed, A resident) or along M (A and C streamed, B resident), so the
+// host->device copy of slab i+1 and the device->host copy of slab i-1 run
+// while slab i computes.  The slab dimension must be a uniform stride of both
+// streamed tensors, larger than the spread of their other offsets: then every
+// slab of them is one address range, disjoint from the others.
+constexpr int kMaxSlabs = 8;
+constexpr size_t kPipelineMinBytes = size_t(64) << 20;
+constexpr size_t kSlabBytes = size_t(32) << 20;
+
+struct Slabs {
+  bool along_n = true;
+  int count = 0;
+  int64_t width = 0;       // columns (N) or rows (M) per slab, a multiple of 128
+  int64_t x_lo = 0, x_hi = 0, ux = 0;  // streamed operand: offset spread, slab stride
+  int64_t c_lo = 0, c_hi = 0, uc = 0;  // C: offset spread, slab stride
+};
+
+void spread(const std::vector<int64_t>& v, int64_t* lo, int64_t* hi) {
+  *lo = v.empty() ? 0 : *std::min_element(v.begin(), v.end());
+  *hi = v.empty() ? 0 : *std::max_element(v.begin(), v.end());
+}
+
+bool plan_slabs(const HostPlan& hp, size_t es, Slabs* sl) {
+  if (hp.batch != 1 || hp.M <= 0 || hp.N <= 0 || hp.K <= 0) return false;
+  int64_t bl, bh, al, ah, cnl, cnh, cml, cmh;
+  spread(hp.rsB, &bl, &bh);   // B offsets of one column (over K)
+  spread(hp.csA, &al, &ah);   // A offsets of one row (over K)
+  spread(hp.rsC, &cml, &cmh); // C offsets of one column (over M)
+  spread(hp.csC, &cnl, &cnh); // C offsets of one row (over N)
+  const bool n_ok = hp.N >= 256 && hp.uB_n >= 1 && hp.uC_n >= 1 && bh - bl < hp.uB_n &&
+                    cmh - cml < hp.uC_n;
+  const bool m_ok = hp.M >= 256 && hp.uA_m >= 1 && hp.uC_m >= 1 && ah - al < hp.uA_m &&
+                    cnh - cnl < hp.uC_m;
+  if (!n_ok && !m_ok) return false;
+  sl->along_n = n_ok;
+  const int64_t len = n_ok ? hp.N : hp.M;
+  const size_t streamed = size_t(n_ok ? hp.spanB : hp.spanA) * es + size_t(hp.spanC) * es;
+  int64_t count = std::max<int64_t>(2, std::min<int64_t>(kMaxSlabs, streamed / kSlabBytes));
+  sl->width = ((len + count - 1) / count + 127) / 128 * 128;
+  sl->count = static_cast<int>((len + sl->width - 1) / sl->width);
+  if (sl->count < 2) return false;
+  if (n_ok) {
+    sl->x_lo = bl; sl->x_hi = bh; sl->ux = hp.uB_n;
+    sl->c_lo = cml; sl->c_hi = cmh; sl->uc = hp.uC_n;
+  } else {
+    sl->x_lo = al; sl->x_hi = ah; sl->ux = hp.uA_m;
+    sl->c_lo = cnl; sl->c_hi = cnh; sl->uc = hp.uC_m;
+  }
+  return true;
+}
+
+}  // namespace
+
+namespace {
+
+// The slab pipeline (see plan_slabs).  Streams: copy_in (host->device),
+// the context stream (kernels), copy_out (device->host); events order them:
+//   copy_in : [after earlier work on the context stream] resident operand,
+//             then per slab its range of the streamed operand (and of C when
+//             C is read) -> pev[2 + i]
+//   stream  : waits for the resident operand (pev[1]) and pev[2 + i], runs
+//             slab i -> pev[2 + kMaxSlabs + i]
+//   copy_out: waits for pev[2 + kMaxSlabs + i], copies slab i of C back
+// The call returns once copy_out has finished (the result is in host memory).
+int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
+                  const GemmArgs& g0, const t1m_tensor* a, const t1m_tensor* b,
+                  const t1m_tensor* c, const Slabs& sl, bool readC, bool timing,
+                  t1m_report* report) {
+  cudaStream_t s = ctx->stream;
+  const size_t bytesA = size_t(hp.spanA) * es, bytesB = size_t(hp.spanB) * es;
+  const size_t bytesC = size_t(hp.spanC) * es;
+  for (int i = 0; i < 3; ++i)
+    if (int st = ensure_stage(ctx, i, i == 0 ? bytesA : i == 1 ? bytesB : bytesC)) return st;
+  cudaError_t e = cudaSuccess;
+  int64_t h2d = 0, d2h = 0;
+  if (timing) cudaEventRecord(ctx->ev[0], s);
+  // Earlier work on the context stream may still use the staging buffers.
+  cudaEventRecord(ctx->pev[0], s);
+  cudaStreamWaitEvent(ctx->copy_in, ctx->pev[0], 0);
+  cudaStreamWaitEvent(ctx->copy_out, ctx->pev[0], 0);
+  // Resident operand, whole.
+  const int res = sl.along_n ? 0 : 1;
+  const t1m_tensor* rt = sl.along_n ? a : b;
+  const size_t rbytes = sl.along_n ? bytesA : bytesB;
+  if ((e = cudaMemcpyAsync(ctx->stage[res], rt->data, rbytes, cudaMemcpyHostToDevice,
+                           ctx->copy_in)) != cudaSuccess)
+    return cuda_fail(ctx, e, "copy resident operand to device");
+  h2d += static_cast<int64_t>(rbytes);
+  cudaEventRecord(ctx->pev[1], ctx->copy_in);
+  cudaStreamWaitEvent(s, ctx->pev[1], 0);
+
+  const int xs = sl.along_n ? 1 : 0;
+  const t1m_tensor* xt = sl.along_n ? b : a;
+  // A C slab range that holds elements outside C (a strided view) goes to
+  // the device first, so copying the range back leaves them as they were.
+  const bool c_in = readC || hp.spanC != hp.M * hp.N;
+  const int64_t len = sl.along_n ? hp.N : hp.M;
+  int kernels = 0, used_method = method, splits = 1;
+  for (int i = 0; i < sl.count; ++i) {
+    const int64_t lo = i * sl.width, hi = std::min(len, lo + sl.width);
+    // Streamed operand and C: element ranges of this slab.
+    const int64_t x0 = lo * sl.ux + sl.x_lo, x1 = (hi - 1) * sl.ux + sl.x_hi + 1;
+    const int64_t c0 = lo * sl.uc + sl.c_lo, c1 = (hi - 1) * sl.uc + sl.c_hi + 1;
+    const size_t xo = size_t(x0) * es, xn = size_t(x1 - x0) * es;
+    const size_t co = size_t(c0) * es, cn = size_t(c1 - c0) * es;
+    if ((e = cudaMemcpyAsync(static_cast<char*>(ctx->stage[xs]) + xo,
+                             static_cast<const char*>(xt->data) + xo, xn, cudaMemcpyHostToDevice,
+                             ctx->copy_in)) != cudaSuccess)
+      return cuda_fail(ctx, e, "copy slab to device");
+    h2d += static_cast<int64_t>(xn);
+    if (c_in) {
+      if ((e = cudaMemcpyAsync(static_cast<char*>(ctx->stage[2]) + co,
+                               static_cast<const char*>(c->data) + co, cn,
+                               cudaMemcpyHostToDevice, ctx->copy_in)) != cudaSuccess)
+        return cuda_fail(ctx, e, "copy C slab to device");
+      h2d += static_cast<int64_t>(cn);
+    }
+    cudaEventRecord(ctx->pev[2 + i], ctx->copy_in);
+    cudaStreamWaitEvent(s, ctx->pev[2 + i], 0);
+    // The slab as a contraction of its own: the slab dimension shortened
+    // and the streamed operand and C shifted by its first index (uniform
+    // strides, so no scatter vector changes).
+    GemmArgs gs = g0;
+    gs.A = ctx->stage[0];
+    gs.B = ctx->stage[1];
+    gs.C = ctx->stage[2];
+    if (sl.along_n) {
+      gs.N = hi - lo;
+      gs.B = static_cast<const char*>(gs.B) + size_t(lo * hp.uB_n) * es;
+      gs.C = static_cast<char*>(gs.C) + size_t(lo * hp.uC_n) * es;
+    } else {
+      gs.M = hi - lo;
+      gs.A = static_cast<const char*>(gs.A) + size_t(lo * hp.uA_m) * es;
+      gs.C = static_cast<char*>(gs.C) + size_t(lo * hp.uC_m) * es;
+    }
+    gs.k_per_split = hp.K;
+    gs.c_split_stride = 0;
+    if (int st = launch_product(ctx, method, dtype, es, hp, gs, s, &kernels, &used_method, &splits))
+      return st;
+    cudaEventRecord(ctx->pev[2 + kMaxSlabs + i], s);
+    cudaStreamWaitEvent(ctx->copy_out, ctx->pev[2 + kMaxSlabs + i], 0);
+    if ((e = cudaMemcpyAsync(static_cast<char*>(c->data) + co,
+                             static_cast<const char*>(ctx->stage[2]) + co, cn,
+                             cudaMemcpyDeviceToHost, ctx->copy_out)) != cudaSuccess)
+      return cuda_fail(ctx, e, "copy C slab to host");
+    d2h += static_cast<int64_t>(cn);
+  }
+  cudaEventRecord(ctx->pev[2 + 2 * kMaxSlabs], ctx->copy_out);
+  cudaStreamWaitEvent(s, ctx->pev[2 + 2 * kMaxSlabs], 0);
+  if (timing) cudaEventRecord(ctx->ev[3], s);
+  e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "contraction");
+  if (int st = check_device_error(ctx)) return st;
+  if (report) {
+    std::memset(report, 0, sizeof(*report));
+    report->method = used_method;
+    report->split_k = splits;
+    report->m = hp.M;
+    report->n = hp.N;
+    report->k = hp.K;
+    const bool cplx = dtype == T1M_COMPLEX64 || dtype == T1M_COMPLEX128;
+    report->flops = (cplx ? 8.0 : 2.0) * double(hp.M) * double(hp.N) * double(hp.K);
+    report->h2d_bytes = h2d;
+    report->d2h_bytes = d2h;
+    report->kernels = kernels;
+    if (timing) {
+      // Copies and kernels overlap: the whole call is reported as kernel time.
+      float t = 0;
+      cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[3]);
+      report->kernel_ms = t;
+    }
+  }
   return T1M_OK;
 }
 
@@ -292,6 +535,10 @@ int t1m_create(t1m_context** out, int device) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking);
+  for (int i = 0; i < t1m_context::kPipeEvents && e == cudaSuccess; ++i)
+    e = cudaEventCreateWithFlags(&ctx->pev[i], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, 64);
   if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, 64);
   if (e != cudaSuccess) {
@@ -321,6 +568,16 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->work) cudaFree(ctx->work);
+  for (int i = 0; i < t1m_context::kPipeEvents; ++i)
+    if (ctx->pev[i]) cudaEventDestroy(ctx->pev[i]);
+  if (ctx->copy_in) {
+    cudaStreamSynchronize(ctx->copy_in);
+    cudaStreamDestroy(ctx->copy_in);
+  }
+  if (ctx->copy_out) {
+    cudaStreamSynchronize(ctx->copy_out);
+    cudaStreamDestroy(ctx->copy_out);
+  }
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return T1M_OK;
@@ -475,6 +732,20 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
   const bool readC = (g.flags & kFlagAccumulate) || !(g.flags & kFlagBetaZero) || hp.K == 0;
   int64_t h2d = 0, d2h = 0;
   cudaStream_t s = ctx->stream;
+
+  // All operands in host memory and large: slab pipeline (copies overlap the
+  // kernels).  Not with forced split-K, and only where every slab runs
+  // without split-K.
+  Slabs sl;
+  if (!devA && !devB && !devC && ctx->split_k == 0 && bytesA + bytesB + bytesC >= kPipelineMinBytes &&
+      plan_slabs(hp, es, &sl)) {
+    int64_t kps = 0;
+    const int64_t sm = sl.along_n ? hp.M : sl.width, sn = sl.along_n ? sl.width : hp.N;
+    if (method == T1M_METHOD_PLAIN || method == T1M_METHOD_DMMA || tc_supported(method, dtype, hp))
+      if (choose_splits(ctx, method, dtype, sm, sn, hp.K, es, &kps) == 1)
+        return run_pipelined(ctx, method, dtype, es, hp, g, a, b, c, sl, readC, timing, report);
+  }
+
   if (timing) cudaEventRecord(ctx->ev[0], s);
   g.A = a->data;
   g.B = b->data;
@@ -520,55 +791,8 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     g.C = static_cast<char*>(g_all.C) + oc * static_cast<int64_t>(es);
     g.k_per_split = std::max<int64_t>(hp.K, 1);
     g.c_split_stride = 0;
-    int nk = 0;
-    if (hp.K == 0) {
-      // C <- beta*C (or unchanged): nothing to multiply; handled by the plain
-      // kernel with an empty K loop.
-      e = launch_simt(dtype, g, 1, s, &nk);
-      used_method = T1M_METHOD_PLAIN;
-    } else {
-      const bool dmma_ok =
-          method == T1M_METHOD_DMMA && (dtype == T1M_FLOAT64 || dtype == T1M_COMPLEX128);
-      if (method != T1M_METHOD_PLAIN && !dmma_ok && !tc_supported(method, dtype, hp))
-        return fail(ctx, T1M_ERR_UNSUPPORTED,
-                    std::string("method ") + std::to_string(method) +
-                        " is not available for this dtype/contraction");
-      int64_t kps = hp.K;
-      splits = choose_splits(ctx, method, dtype, hp, es, &kps);
-      // Split-K: the main kernel writes raw partial products (alpha = 1,
-      // beta = 0) into dense workspace slices, m fastest; the reduction sums
-      // them in FP64 and applies the epilogue.
-      GemmArgs gm = g;
-      if (splits > 1) {
-        if (int st = ensure_work(ctx, size_t(splits) * size_t(hp.M) * size_t(hp.N) * es)) return st;
-        gm.C = ctx->work;
-        gm.rsC = nullptr;
-        gm.csC = nullptr;
-        gm.uC_m = 1;
-        gm.uC_n = hp.M;
-        gm.alpha[0] = 1.0;
-        gm.alpha[1] = 0.0;
-        gm.beta[0] = gm.beta[1] = 0.0;
-        gm.flags = (g.flags & (kFlagConjA | kFlagConjB)) | kFlagBetaZero;
-        gm.k_per_split = kps;
-        gm.c_split_stride = hp.M * hp.N;
-      }
-      if (method == T1M_METHOD_PLAIN) {
-        e = launch_simt(dtype, gm, splits, s, &nk);
-      } else if (method == T1M_METHOD_DMMA) {
-        e = launch_dmma(dtype, gm, splits, s, &nk);
-      } else {
-        std::string err;
-        e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err);
-        if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
-      }
-      if (e == cudaSuccess && splits > 1) {
-        e = launch_splitk_reduce(dtype, ctx->work, splits, g, s);
-        ++nk;
-      }
-    }
-    kernels += nk;
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel launch");
+    if (int st = launch_product(ctx, method, dtype, es, hp, g, s, &kernels, &used_method, &splits))
+      return st;
   }
   if (timing) cudaEventRecord(ctx->ev[2], s);
   if (!devC && bytesC) {

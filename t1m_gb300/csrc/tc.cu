@@ -751,8 +751,11 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         const uint32_t b0 = rb + bsrc0;
 #pragma unroll
         for (int j = 0; j < 4; ++j) bv[j] = lds128(b0 + kBStep * j);
-        __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(raw_empty(rr));
+        // The raw stage is released after the conversion (below), once the
+        // values read from it are consumed and behind the cross-proxy fence:
+        // TMA (async proxy) refills it, and generic-proxy reads that are not
+        // ordered before that by a proxy fence can observe the refill.
+        const int r_cur = static_cast<int>(rr);
         if (++rr == kRaw) {
           rr = 0;
           rph ^= 1u;
@@ -807,7 +810,10 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         ptx::fence_proxy_async_smem();
         ptx::tc_fence_before();
         __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(full_bar(st));
+        if (lane == 0) {
+          ptx::mbar_arrive(full_bar(st));
+          ptx::mbar_arrive(raw_empty(r_cur));
+        }
         if (++st == kStages) {
           st = 0;
           sph ^= 1u;
@@ -1232,8 +1238,10 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           }
         }
       }
-      __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(raw_empty(r));
+      // The raw stage is released after the conversion (below), once the
+      // values read from it are consumed and behind the cross-proxy fence:
+      // TMA (async proxy) refills it, and generic-proxy reads that are not
+      // ordered before that by a proxy fence can observe the refill.
 
       if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
         record_error(err_flag, kErrEmptyWait);
@@ -1322,7 +1330,10 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       ptx::fence_proxy_async_smem();
       ptx::tc_fence_before();
       __syncwarp();
-      if (lane == 0) ptx::mbar_arrive(full_bar(st));
+      if (lane == 0) {
+        ptx::mbar_arrive(full_bar(st));
+        ptx::mbar_arrive(raw_empty(r));
+      }
 
       // Fold the previous chunk once the first stage of the next is queued.
       if ((s % kFold) == 0 && s >= kFold) {
