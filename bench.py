@@ -57,11 +57,16 @@ def _peaks() -> dict:
             "sm_max_mhz": 2070.0, "_source": "fallback"}
 
 
-def _profiled_traffic():
-    """DRAM bytes (read + write) per launch of the tensor-core kernel on this
-    workload, from the committed ncu summary (None if absent)."""
-    p = ROOT / "profiles" / "tc1m_contract_ijkl_klmn_64.md"
-    if not p.exists():
+PROFILE_OF = {"tc_3xtf32": "tc1m_contract_ijkl_klmn_64.md",
+              "tc_bf16x6": "tc1m_contract_bf16x6_ijkl_klmn_64.md"}
+
+
+def _profiled_traffic(method):
+    """DRAM bytes (read + write) per launch of the tensor-core kernel of
+    `method` on this workload, from the committed ncu summary (None if absent)."""
+    name = PROFILE_OF.get(method)
+    p = ROOT / "profiles" / name if name else None
+    if p is None or not p.exists():
         return None
     for line in p.read_text().splitlines():
         if line.startswith("dram_bytes_per_launch"):
@@ -252,14 +257,13 @@ def run_gpu(args) -> None:
         ctx.set_method(method_name)
         return t1m.contract_scaled(1.0, ta, LA, tb, LB, 0.0, tc, LC, ctx=ctx)
 
-    # Method of the tensor-core arm: 3xTF32 if this build has it.
+    # Method of the tensor-core arm: the library's automatic choice (BF16x6
+    # or 3xTF32 for this layout), reported by the method that ran.
     tc_method = args.method
+    rep0 = one(tc_method)
+    ran = t1m.method(rep0.method).name
     if tc_method == "auto":
-        try:
-            one("tc_3xtf32")
-            tc_method = "tc_3xtf32"
-        except t1m.T1MError:
-            tc_method = "plain"
+        tc_method = ran
     torch.cuda.synchronize()
     err_tc = _sampled_error(torch, ga, gb, gc)
 
@@ -353,6 +357,11 @@ def run_gpu(args) -> None:
             peak = peaks["bf16_tflops"] / 2.0 / 3.0
             peak_note = ("TF32 dense = measured bf16 burst / 2, divided by the 3 TF32 "
                          f"products per algorithmic flop ({peaks['_source']})")
+        elif tc_method in ("tc_bf16x6", "tc_bf16x3"):
+            nprod = 6.0 if tc_method == "tc_bf16x6" else 3.0
+            peak = peaks["bf16_tflops"] / nprod
+            peak_note = (f"measured bf16 burst divided by the {int(nprod)} bf16 products per "
+                         f"algorithmic flop ({peaks['_source']})")
         else:
             peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
             peak_note = "FP32 SIMT nominal 152 SM x 128 lanes x 2 x max SM clock"
@@ -374,8 +383,8 @@ def run_gpu(args) -> None:
             "roofline": {"bound": "tensor" if tc_method != "plain" else "fp32-simt",
                          "achieved": kernel_tflops, "peak": peak, "unit": "TFLOP/s",
                          "frac": kernel_tflops / peak,
-                         "traffic": _profiled_traffic() if tc_method == "tc_3xtf32" else None,
-                         "traffic_source": "profiles/tc1m_contract_ijkl_klmn_64.md (ncu dram bytes "
+                         "traffic": _profiled_traffic(tc_method),
+                         "traffic_source": f"profiles/{PROFILE_OF.get(tc_method)} (ncu dram bytes "
                                            "read+write per launch)",
                          "peak_note": peak_note},
             "e2e": {"value": world * FLOPS / e2e_s / 1e12, "unit": "TFLOP/s",

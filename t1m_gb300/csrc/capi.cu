@@ -29,7 +29,7 @@ namespace t1m {
 namespace gb300 {
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args,
                       const HostPlan& plan, int splits, cudaStream_t stream,
-                      int* err_flag, int* kernels, std::string* err);
+                      int* err_flag, int* kernels, std::string* err, int* used_method);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
 void tc_tile(int* bm, int* bn, int* bk);
 cudaError_t launch_dmma(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
@@ -193,9 +193,9 @@ int check_device_error(t1m_context* ctx) {
 int choose_method(const t1m_context* ctx, int dtype, const HostPlan& plan) {
   int m = ctx->method;
   if (m != T1M_METHOD_AUTO) return m;
-  if (dtype == T1M_COMPLEX64 && tc_supported(T1M_METHOD_TC_3XTF32, dtype, plan) &&
+  if (dtype == T1M_COMPLEX64 && tc_supported(kMethodTcAuto, dtype, plan) &&
       plan.M * plan.N * plan.K >= int64_t(1) << 18)
-    return T1M_METHOD_TC_3XTF32;
+    return kMethodTcAuto;
   return T1M_METHOD_PLAIN;
 }
 
@@ -299,7 +299,9 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       e = launch_dmma(dtype, gm, splits, s, &nk);
     } else {
       std::string err;
-      e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err);
+      int ran = method;
+      e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran);
+      *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
     if (e == cudaSuccess && splits > 1) {

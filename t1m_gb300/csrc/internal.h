@@ -106,6 +106,11 @@ constexpr uint32_t kFlagBetaZero = 16u;  // BLAS semantics with beta == 0
 constexpr uint32_t kFlagCPairs = 32u;
 constexpr uint32_t kFlagCCol16 = 64u;
 
+// Internal method id: tensor cores, precision chosen per problem by the
+// launcher (BF16x6 where the one-tile kernel fetches both operands by TMA,
+// 3xTF32 elsewhere); the report carries the method that ran.
+constexpr int kMethodTcAuto = 100;
+
 // Launchers.  Return cudaError_t of the launch.
 // simt.cu: plain FP32/FP64 kernel; `splits` CTA rows along K.
 cudaError_t launch_simt(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,

@@ -39,7 +39,7 @@ namespace t1m {
 namespace gb300 {
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
-                      std::string* err);
+                      std::string* err, int* used_method);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
 void tc_tile(int* bm, int* bn, int* bk);
 cudaError_t launch_dmma(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
@@ -290,7 +290,7 @@ extern "C" int t1m_contract_noalloc(void* stream_ptr, int method, int dtype, con
       e = launch_dmma(dtype, gm, splits, stream, &kernels);
     } else {
       std::string lerr;
-      e = launch_tc(method, dtype, gm, hp, splits, stream, err_word, &kernels, &lerr);
+      e = launch_tc(method, dtype, gm, hp, splits, stream, err_word, &kernels, &lerr, nullptr);
       if (e != cudaSuccess && !lerr.empty()) return finish(err, err_len, T1M_ERR_CUDA, lerr);
     }
     if (e == cudaSuccess && splits > 1) e = launch_splitk_reduce(dtype, partials, splits, g, stream);

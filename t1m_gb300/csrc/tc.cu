@@ -1553,7 +1553,7 @@ void tc_tile(int* bm, int* bn, int* bk) {
 bool tc_supported(int method, int dtype, const HostPlan& plan) {
   (void)plan;
   return (method == T1M_METHOD_TC_3XTF32 || method == T1M_METHOD_TC_BF16X3 ||
-          method == T1M_METHOD_TC_BF16X6) &&
+          method == T1M_METHOD_TC_BF16X6 || method == kMethodTcAuto) &&
          dtype == T1M_COMPLEX64;
 }
 
@@ -1657,8 +1657,9 @@ cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_g
 
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
-                      std::string* err) {
+                      std::string* err, int* used_method) {
   *kernels = 0;
+  if (used_method) *used_method = method;
   if (!tc_supported(method, dtype, plan)) {
     *err = "tensor-core method not available for this dtype";
     return cudaErrorNotSupported;
@@ -1672,6 +1673,15 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   p.dep = -1;
   cudaError_t e;
+  if (method == kMethodTcAuto) {
+    // BF16x6 measured faster than 3xTF32 (203 vs 193-198 TFLOP/s at complex64
+    // 4096^3) and more accurate in the one-tile kernel with TMA operands;
+    // block-TMA layouts stay on the persistent 3xTF32 kernel.
+    const bool tma_both = p.block_maps == 0 && p.amode != kAMK16 && p.amode != kAGather &&
+                          p.bmode != kBGather;
+    method = tma_both ? T1M_METHOD_TC_BF16X6 : T1M_METHOD_TC_3XTF32;
+    if (used_method) *used_method = method;
+  }
   const bool bf16 = method != T1M_METHOD_TC_3XTF32;
   if (bf16 || (p.block_maps == 0 && p.amode != kAMK16)) {
     // Uniform or gathered operands: the one-tile-per-CTA form.  The bf16
