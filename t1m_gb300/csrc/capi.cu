@@ -31,7 +31,7 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args,
                       const HostPlan& plan, int splits, cudaStream_t stream,
                       int* err_flag, int* kernels, std::string* err, int* used_method);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
-void tc_tile(int* bm, int* bn, int* bk);
+void tc_tile(int dtype, int* bm, int* bn, int* bk);
 cudaError_t launch_dmma(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
                         int* kernels);
 void dmma_tile(int* bm, int* bn, int* bk);
@@ -193,8 +193,8 @@ int check_device_error(t1m_context* ctx) {
 int choose_method(const t1m_context* ctx, int dtype, const HostPlan& plan) {
   int m = ctx->method;
   if (m != T1M_METHOD_AUTO) return m;
-  if (dtype == T1M_COMPLEX64 && tc_supported(kMethodTcAuto, dtype, plan) &&
-      plan.M * plan.N * plan.K >= int64_t(1) << 18)
+  if ((dtype == T1M_COMPLEX64 || dtype == T1M_FLOAT32) && tc_supported(kMethodTcAuto, dtype, plan) &&
+      plan.M * plan.N * plan.K >= int64_t(1) << (dtype == T1M_FLOAT32 ? 20 : 18))
     return kMethodTcAuto;
   return T1M_METHOD_PLAIN;
 }
@@ -216,7 +216,7 @@ int choose_splits(const t1m_context* ctx, int method, int dtype, int64_t M, int6
     dmma_tile(&bm, &bn, &bk);
     per_sm = 8;
   } else {
-    tc_tile(&bm, &bn, &bk);
+    tc_tile(dtype, &bm, &bn, &bk);
     per_sm = 1;
   }
   const int64_t tiles = ((M + bm - 1) / bm) * ((N + bn - 1) / bn);
@@ -906,7 +906,7 @@ constexpr size_t kGroupItemWorkBytes = size_t(256) << 20;
 int group_splits(int dtype, int fam, const HostPlan& hp, size_t es, int64_t* k_per_split) {
   int bm = 0, bn = 0, bk = 0;
   if (fam == kFamTC) {
-    tc_tile(&bm, &bn, &bk);
+    tc_tile(dtype, &bm, &bn, &bk);
   } else {
     simt_tile(dtype, &bm, &bn, &bk);
     if (fam == kFamSimtSkinny) bk = 16;

@@ -41,7 +41,7 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
-void tc_tile(int* bm, int* bn, int* bk);
+void tc_tile(int dtype, int* bm, int* bn, int* bk);
 cudaError_t launch_dmma(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
                         int* kernels);
 void dmma_tile(int* bm, int* bn, int* bk);
@@ -253,7 +253,7 @@ extern "C" int t1m_contract_noalloc(void* stream_ptr, int method, int dtype, con
       dmma_tile(&bm, &bn, &bk);
       per_sm = 8;
     } else {
-      tc_tile(&bm, &bn, &bk);
+      tc_tile(dtype, &bm, &bn, &bk);
       per_sm = 1;
     }
     int sms = 152;

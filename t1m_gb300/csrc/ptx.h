@@ -253,6 +253,13 @@ __device__ __forceinline__ void cp_async_8(uint32_t dst, const void* src, uint32
                : "memory");
 }
 
+// 4-byte form (real float32 elements).
+__device__ __forceinline__ void cp_async_4(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+
 // Arrive on `bar` once all prior cp.async of this thread have landed (the
 // arrival counts against the barrier's initial count).
 __device__ __forceinline__ void cp_async_arrive_noinc(uint32_t bar) {

@@ -179,6 +179,11 @@ __device__ __forceinline__ void split_bf16(float x, float y, uint32_t& w0, uint3
   }
 }
 
+__device__ __forceinline__ float lds32(uint32_t addr) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+  return v;
+}
 __device__ __forceinline__ float2 lds64(uint32_t addr) {
   float2 v;
   asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(addr));
@@ -278,6 +283,76 @@ __device__ __forceinline__ void gather_b_stage(const GemmArgs& g, uint32_t dst, 
   }
 }
 
+// Real (float32) gathers, 4-byte cp.async.  A raw tile [k][m]: 32 k x 128 m
+// floats, 512-byte rows (consecutive threads walk m); B raw tile [n][k]:
+// 128 n x 32 k floats in 128-byte swizzled rows, the same bytes as the
+// complex [n][k] tile (k pairs take the place of complex elements).  B:
+// thread lt always takes k = lt % 32 (96 is a multiple of 32), n = lt / 32 + 3 i.
+template <int kBatch>
+__device__ __forceinline__ void gather_a_stage_real(const GemmArgs& g, uint32_t dst, int lt,
+                                                    int64_t m0, int64_t k0, int64_t ke) {
+  const float* __restrict__ A = static_cast<const float*>(g.A);
+  const int64_t* __restrict__ rsA = g.rsA;
+  const int64_t* __restrict__ csA = g.csA;
+  const int64_t uA_m = g.uA_m, uA_k = g.uA_k, M = g.M;
+  constexpr int kElems = 128 * 32;
+  constexpr int kPer = (kElems + kLoaders - 1) / kLoaders;  // 43
+#pragma unroll 1
+  for (int i0 = 0; i0 < kPer; i0 += kBatch) {
+    const float* src[kBatch];
+    uint32_t okm = 0;
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int e = lt + kLoaders * (i0 + j);
+      const int m = e % 128, k = e / 128;
+      const bool in = (i0 + j < kPer) && e < kElems && (m0 + m < M) && (k0 + k < ke);
+      src[j] = in ? A + offs(rsA, uA_m, m0 + m) + offs(csA, uA_k, k0 + k) : A;
+      okm |= in ? (1u << j) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int e = lt + kLoaders * (i0 + j);
+      if (i0 + j < kPer && e < kElems) {
+        const int m = e % 128, k = e / 128;
+        ptx::cp_async_4(dst + static_cast<uint32_t>(k * 512 + m * 4), src[j],
+                        ((okm >> j) & 1u) ? 4u : 0u);
+      }
+    }
+  }
+}
+
+template <int kBatch>
+__device__ __forceinline__ void gather_b_stage_real(const GemmArgs& g, uint32_t dst, int lt,
+                                                    int64_t n0, int64_t k0, int64_t ke) {
+  const float* __restrict__ B = static_cast<const float*>(g.B);
+  const int64_t* __restrict__ csB = g.csB;
+  const int64_t uB_n = g.uB_n, N = g.N;
+  const int k = lt & 31;
+  const bool kin = k0 + k < ke;
+  const int64_t rk = kin ? offs(g.rsB, g.uB_k, k0 + k) : 0;
+  constexpr int kStride = kLoaders / 32;                 // 3
+  constexpr int kPer = (kTileN + kStride - 1) / kStride; // 43
+#pragma unroll 1
+  for (int i0 = 0; i0 < kPer; i0 += kBatch) {
+    const float* src[kBatch];
+    uint32_t okm = 0;
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int n = (lt >> 5) + kStride * (i0 + j);
+      const bool in = kin && (i0 + j < kPer) && n < kTileN && (n0 + n < N);
+      src[j] = in ? B + rk + offs(csB, uB_n, n0 + n) : B;
+      okm |= in ? (1u << j) : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kBatch; ++j) {
+      const int n = (lt >> 5) + kStride * (i0 + j);
+      if (i0 + j < kPer && n < kTileN)
+        ptx::cp_async_4(dst + swz128(n, k >> 1) + 4u * (k & 1), src[j],
+                        ((okm >> j) & 1u) ? 4u : 0u);
+    }
+  }
+}
+
 // Epilogue of one converter thread: accumulator columns [col0, col0 + kCols)
 // of real row 2 ci + part (part 0 holds the real parts of complex row ci,
 // part 1 the imaginary parts).  Lane pairs swap halves with two shuffles per
@@ -355,6 +430,63 @@ __device__ __forceinline__ void store_tile(const GemmArgs& g, float2* __restrict
           const float2 o1 = *p1;
           *p1 = make_float2(t1r + (br * o1.x - bi * o1.y), t1i + (br * o1.y + bi * o1.x));
         }
+      }
+    }
+  }
+}
+
+// Real epilogue: accumulator columns [col0, col0 + kCols) of real row `row`
+// (one TMEM lane per row, no pairing).  For real problems kFlagCPairs means
+// four consecutive columns contiguous and 16-byte aligned: one 16-byte store
+// per four values.  kFlagCCol16 as in store_tile.
+template <int kCols>
+__device__ __forceinline__ void store_tile_real(const GemmArgs& g, float* __restrict__ Cp,
+                                                int64_t row, bool row_ok, int64_t n0, int col0,
+                                                const float (&master)[kCols]) {
+  if (!row_ok) return;
+  const uint32_t flags = g.flags;
+  const bool accumulate = flags & kFlagAccumulate;
+  const bool beta_zero = flags & kFlagBetaZero;
+  const bool quads = flags & kFlagCPairs;
+  const bool col16 = flags & kFlagCCol16;
+  const float ar = (float)g.alpha[0], br = (float)g.beta[0];
+  const int64_t N = g.N;
+  const int64_t* __restrict__ csC = g.csC;
+  const int64_t uC_n = g.uC_n;
+  float* __restrict__ Cr = Cp + offs(g.rsC, g.uC_m, row);
+  int64_t blk = 0;
+#pragma unroll
+  for (int q = 0; q < kCols / 4; ++q) {
+    const int c = col0 + 4 * q;
+    const int64_t n = n0 + c;
+    if (col16 && (q & 3) == 0) {
+      const int64_t nb = n0 + col0 + 16 * (q >> 2);
+      blk = nb < N ? offs(csC, uC_n, nb) : 0;
+    }
+    if (n >= N) continue;
+    const int64_t on = col16 ? blk + (c - col0 - 16 * (q >> 2)) : offs(csC, uC_n, n);
+    float t[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) t[i] = ar * master[4 * q + i];
+    if (quads && n + 3 < N) {
+      float4* p4 = reinterpret_cast<float4*>(Cr + on);
+      if (accumulate) {
+        const float4 o = *p4;
+        *p4 = make_float4(o.x + t[0], o.y + t[1], o.z + t[2], o.w + t[3]);
+      } else if (beta_zero) {
+        *p4 = make_float4(t[0], t[1], t[2], t[3]);
+      } else {
+        const float4 o = *p4;
+        *p4 = make_float4(t[0] + br * o.x, t[1] + br * o.y, t[2] + br * o.z, t[3] + br * o.w);
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        if (n + i >= N) break;
+        float* p = Cr + (col16 ? on + i : (i == 0 ? on : offs(csC, uC_n, n + i)));
+        if (accumulate) *p += t[i];
+        else if (beta_zero) *p = t[i];
+        else *p = t[i] + br * *p;
       }
     }
   }
@@ -945,7 +1077,18 @@ constexpr int kBP1 = (kTileN * kStepK / 2) / kConverters1;   // 16-byte B pieces
 constexpr int kB16P1 = (kTileN * kStepK / 4) / kConverters1; // bf16 B chunks per thread
 static_assert(kAK1 % 4 == 0 && kMC1 % 16 == 0 && kBP1 >= 1 && kB16P1 >= 1, "converter split");
 
-template <int AMode, int BMode, int Prec>
+// Real float32 (kReal): the same GEMM without the 1M expansion.  A tile is
+// 128 real rows (one TMEM lane each), K is staged 32 reals per stage (the
+// same 128-byte swizzle rows), the raw A stage doubles to 16 KB, B's raw
+// bytes are the complex layout's (k pairs for complex elements), and the
+// epilogue writes one real row per thread.
+template <bool kReal>
+constexpr int smem_bytes_1() {
+  return 1024 + kRaw * ((kReal ? 16384 : kRawABytes) + kRawBBytes) + kStages * kOpBytes +
+         kBarrierBytes;
+}
+
+template <int AMode, int BMode, int Prec, bool kReal>
 __global__ void __launch_bounds__(kThreads1, 1)
 tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
   constexpr bool kBF16 = Prec != kPrecTF32x3;
@@ -954,19 +1097,24 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   constexpr bool kTmaA = AMode != kGatherMK;
   constexpr bool kTmaB = BMode != kGatherNK;
   constexpr bool kGather = !kTmaA || !kTmaB;
+  constexpr int kRowsT = kReal ? 128 : kTileMc;        // C rows per tile
+  constexpr int kStepKE = kReal ? 32 : kStepK;         // K elements per stage
+  constexpr int kCx = kReal ? 1 : 2;                   // floats per element (TMA coordinates)
+  constexpr int kRawABytesT = kReal ? 16384 : kRawABytes;
+  constexpr int kRawBytesT = kRawABytesT + kRawBBytes;
   // Arrivals per raw stage: one expect_tx arrive from the TMA thread, one
   // cp.async completion arrive per gather thread.
   constexpr uint32_t kRawArrivals = (kTmaA || kTmaB ? 1u : 0u) + (kGather ? kLoaders : 0u);
-  constexpr uint32_t kTmaBytes = (kTmaA ? kRawABytes : 0) + (kTmaB ? kRawBBytes : 0);
+  constexpr uint32_t kTmaBytes = (kTmaA ? kRawABytesT : 0) + (kTmaB ? kRawBBytes : 0);
 
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const uint32_t base = (ptx::smem_u32(smem_raw) + 1023u) & ~1023u;
   uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
-  const uint32_t raw0 = base;                          // kRaw x (A 8 KB | B 16 KB)
-  const uint32_t op0 = raw0 + kRaw * kRawBytes;        // kStages x (B hi | B lo)
+  const uint32_t raw0 = base;                          // kRaw x (A | B 16 KB)
+  const uint32_t op0 = raw0 + kRaw * kRawBytesT;       // kStages x (B hi | B lo)
   const uint32_t bars = op0 + kStages * kOpBytes;
-  auto raw_a = [&](int r) { return raw0 + r * kRawBytes; };
-  auto raw_b = [&](int r) { return raw0 + r * kRawBytes + kRawABytes; };
+  auto raw_a = [&](int r) { return raw0 + r * kRawBytesT; };
+  auto raw_b = [&](int r) { return raw0 + r * kRawBytesT + kRawABytesT; };
   auto raw_full = [&](int r) { return bars + 8u * r; };
   auto raw_empty = [&](int r) { return bars + 8u * (kRaw + r); };
   auto full_bar = [&](int s) { return bars + 8u * (2 * kRaw + s); };
@@ -1013,7 +1161,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   // Split-K: this CTA row covers K range [kb, K) (kb a multiple of kStepK).
   const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
   const int64_t K = min(args.K, kb + args.k_per_split);
-  const int64_t tiles_m = (M + kTileMc - 1) / kTileMc;
+  const int64_t tiles_m = (M + kRowsT - 1) / kRowsT;
   const int64_t tiles_n = (N + kTileN - 1) / kTileN;
   // Groups of 16 M-tiles sweep N so CTAs running together share B in L2.
   constexpr int64_t G = 16;
@@ -1023,8 +1171,8 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   const int64_t gsize = min(G, tiles_m - first_m);
   const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
   const int64_t tn = (t % (G * tiles_n)) / gsize;
-  const int64_t m0 = tm * kTileMc, n0 = tn * kTileN;
-  const int64_t ksteps = (K - kb + kStepK - 1) / kStepK;
+  const int64_t m0 = tm * kRowsT, n0 = tn * kTileN;
+  const int64_t ksteps = (K - kb + kStepKE - 1) / kStepKE;
 
   if (warp == 0) {
     // ---------------------------------------------------------- MMA issue ---
@@ -1097,7 +1245,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     for (int64_t s = 0; s < ksteps; ++s) {
       const int r = static_cast<int>(s % kRaw);
       const uint32_t ph = static_cast<uint32_t>((s / kRaw) & 1);
-      const int64_t k0 = kb + s * kStepK;
+      const int64_t k0 = kb + s * kStepKE;
       if (kGather || lt == 0) {
         if (!ptx::mbar_wait(raw_empty(r), ph ^ 1u)) {
           record_error(err_flag, kErrRawWait);
@@ -1107,17 +1255,22 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       if ((kTmaA || kTmaB) && lt == 0) {
         ptx::mbar_arrive_expect_tx(raw_full(r), kTmaBytes);
         if (AMode == kTmaMK)
-          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * m0), static_cast<int>(k0), raw_full(r));
+          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(kCx * m0), static_cast<int>(k0), raw_full(r));
         if (AMode == kTmaKM)
-          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(2 * k0), static_cast<int>(m0), raw_full(r));
+          ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(kCx * k0), static_cast<int>(m0), raw_full(r));
         if (BMode == kTmaNK)
-          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * k0), static_cast<int>(n0), raw_full(r));
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(kCx * k0), static_cast<int>(n0), raw_full(r));
         if (BMode == kTmaKN)
-          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(2 * n0), static_cast<int>(k0), raw_full(r));
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(kCx * n0), static_cast<int>(k0), raw_full(r));
       }
       if (kGather) {
-        if (AMode == kGatherMK) gather_a_stage<8>(args, raw_a(r), lt, m0, k0, K);
-        if (BMode == kGatherNK) gather_b_stage<8>(args, raw_b(r), lt, n0, k0, K);
+        if constexpr (kReal) {
+          if (AMode == kGatherMK) gather_a_stage_real<8>(args, raw_a(r), lt, m0, k0, K);
+          if (BMode == kGatherNK) gather_b_stage_real<8>(args, raw_b(r), lt, n0, k0, K);
+        } else {
+          if (AMode == kGatherMK) gather_a_stage<8>(args, raw_a(r), lt, m0, k0, K);
+          if (BMode == kGatherNK) gather_b_stage<8>(args, raw_b(r), lt, n0, k0, K);
+        }
         ptx::cp_async_arrive_noinc(raw_full(r));
       }
     }
@@ -1135,7 +1288,9 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
     const bool conjA = args.flags & kFlagConjA;
     const bool conjB = args.flags & kFlagConjB;
-    const bool row_ok = (m0 + ci) < M;
+    // C row of this thread: complex row ci, or (real) the lane's own row.
+    const int crow = kReal ? rho : ci;
+    const bool row_ok = (m0 + crow) < M;
 
     float master[kMC1];
 #pragma unroll
@@ -1155,11 +1310,14 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
 
     // Loop-invariant shared-memory offsets of this thread's raw reads and
     // operand writes.
+    // Real A: the same 8-byte units of the swizzled [m][k] rows (k pairs),
+    // row = the lane; [k][m] rows of 128 floats.
     uint32_t aoff[kAK1];
 #pragma unroll
     for (int j = 0; j < kAK1; ++j)
-      aoff[j] = (AMode == kTmaKM) ? swz128(ci, kAK1 * wg + 2 * (j >> 1))
+      aoff[j] = (AMode == kTmaKM) ? swz128(crow, kAK1 * wg + 2 * (j >> 1))
                                   : static_cast<uint32_t>((kAK1 * wg + j) * 512 + ci * 8);
+    const uint32_t areal = static_cast<uint32_t>(2 * kAK1 * wg * 512 + rho * 4);
     // TF32 B: piece j of this thread (id = pt + kConverters1 j) is two complex
     // k of one column ([n][k] tiles) or one k of two columns ([k][n] tile).
     uint32_t bsrc[kBP1], boff[kBP1][2];
@@ -1167,8 +1325,10 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     for (int j = 0; j < kBP1; ++j) {
       const int id = pt + kConverters1 * j;
       if (BMode == kTmaKN) {
+        // k: complex k, or (real) the k pair 2k, 2k + 1 (rows of 128 floats).
         const int k = id >> 6, n = 2 * (id & 63);
-        bsrc[j] = static_cast<uint32_t>(k * 1024 + n * 8);
+        bsrc[j] = kReal ? static_cast<uint32_t>(2 * k * 512 + n * 4)
+                        : static_cast<uint32_t>(k * 1024 + n * 8);
         boff[j][0] = swz128(n, k);
         boff[j][1] = swz128(n + 1, k);
       } else {
@@ -1189,7 +1349,10 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     for (int j = 0; j < kB16P1; ++j) {
       const int id = pt + kConverters1 * j;
       const int n = id & 127, kq = id >> 7;
-      b16src[j] = (BMode == kTmaKN) ? static_cast<uint32_t>(4 * kq * 1024 + n * 8) : swz128(n, 4 * kq);
+      b16src[j] = (BMode == kTmaKN)
+                      ? (kReal ? static_cast<uint32_t>(8 * kq * 512 + n * 4)
+                               : static_cast<uint32_t>(4 * kq * 1024 + n * 8))
+                      : swz128(n, 4 * kq);
       b16row[j] = static_cast<uint32_t>((n >> 3) * 1024 + (n & 7) * 128);
       b16chunk[j] = static_cast<uint32_t>(kq ^ (n & 7));
     }
@@ -1206,6 +1369,8 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       }
       // A: kAK1 complex k (this warpgroup's share of the step) of row ci.
       const uint32_t ra = raw_a(r), rb = raw_b(r);
+      // Complex: av[j] = (re, im) of complex k.  Real: av[j] = values of the
+      // k pair 2j, 2j + 1 of the lane's row.
       float2 av[kAK1];
       if (AMode == kTmaKM) {
 #pragma unroll
@@ -1214,6 +1379,10 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           av[2 * j] = make_float2(v.x, v.y);
           av[2 * j + 1] = make_float2(v.z, v.w);
         }
+      } else if constexpr (kReal) {
+#pragma unroll
+        for (int j = 0; j < kAK1; ++j)
+          av[j] = make_float2(lds32(ra + areal + 1024u * j), lds32(ra + areal + 1024u * j + 512u));
       } else {
 #pragma unroll
         for (int j = 0; j < kAK1; ++j) av[j] = lds64(ra + aoff[j]);
@@ -1222,11 +1391,26 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       float4 bv[kBV];
       if constexpr (!kBF16) {
 #pragma unroll
-        for (int j = 0; j < kBP1; ++j) bv[j] = lds128(rb + bsrc[j]);
+        for (int j = 0; j < kBP1; ++j) {
+          if (kReal && BMode == kTmaKN) {
+            // Columns n, n + 1 of rows 2k, 2k + 1: pair (2k, 2k + 1) of each column.
+            const float2 t0 = lds64(rb + bsrc[j]), t1 = lds64(rb + bsrc[j] + 512u);
+            bv[j] = make_float4(t0.x, t1.x, t0.y, t1.y);
+          } else {
+            bv[j] = lds128(rb + bsrc[j]);
+          }
+        }
       } else {
 #pragma unroll
         for (int j = 0; j < kB16P1; ++j) {
-          if (BMode == kTmaKN) {
+          if (kReal && BMode == kTmaKN) {
+            // Column n, real k 8 kq .. 8 kq + 7 (rows of 128 floats).
+            float v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = lds32(rb + b16src[j] + 512u * i);
+            bv[2 * j] = make_float4(v[0], v[1], v[2], v[3]);
+            bv[2 * j + 1] = make_float4(v[4], v[5], v[6], v[7]);
+          } else if (BMode == kTmaKN) {
             const float2 t0 = lds64(rb + b16src[j]), t1 = lds64(rb + b16src[j] + 1024u);
             const float2 t2 = lds64(rb + b16src[j] + 2048u), t3 = lds64(rb + b16src[j] + 3072u);
             bv[2 * j] = make_float4(t0.x, t0.y, t1.x, t1.y);
@@ -1259,8 +1443,9 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           float2 v = av[j];
           if (conjA) v.y = -v.y;
           if (!row_ok) v = make_float2(0.f, 0.f);
-          const float x0 = part ? v.y : v.x;
-          const float x1 = part ? v.x : -v.y;
+          // 1M rows [re, -im] (part 0) / [im, re] (part 1); real: the pair as is.
+          const float x0 = kReal ? v.x : (part ? v.y : v.x);
+          const float x1 = kReal ? v.y : (part ? v.x : -v.y);
           split_bf16<kPieces>(x0, x1, w[0][j], w[1][j], w[2][j]);
         }
         const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + kAK1 * wg;
@@ -1294,8 +1479,9 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           float2 v = av[j];
           if (conjA) v.y = -v.y;
           if (!row_ok) v = make_float2(0.f, 0.f);
-          const float x0 = part ? v.y : v.x;
-          const float x1 = part ? v.x : -v.y;
+          // 1M rows [re, -im] (part 0) / [im, re] (part 1); real: the pair as is.
+          const float x0 = kReal ? v.x : (part ? v.y : v.x);
+          const float x1 = kReal ? v.y : (part ? v.x : -v.y);
           const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
           hi[2 * j] = s0.hi;
           lo[2 * j] = s0.lo;
@@ -1371,9 +1557,15 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       const int64_t c_last = (ksteps - 1) / kFold;
       fold_from((c_last & 1) ? kChunkCol1 : kChunkCol0);
       fold_from(kCorrCol);
-      float2* __restrict__ Cp =
-          static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
-      store_tile<kMC1>(args, Cp, m0 + ci, row_ok, n0, wg * kMC1, part, master);
+      if constexpr (kReal) {
+        float* __restrict__ Cp =
+            static_cast<float*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
+        store_tile_real<kMC1>(args, Cp, m0 + rho, row_ok, n0, wg * kMC1, master);
+      } else {
+        float2* __restrict__ Cp =
+            static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
+        store_tile<kMC1>(args, Cp, m0 + ci, row_ok, n0, wg * kMC1, part, master);
+      }
     }
   }
 
@@ -1439,39 +1631,65 @@ bool unit_blocks16(const std::vector<int64_t>& v, int64_t n) {
   return true;
 }
 
-template <int AMode, int BMode, int Prec>
+template <int AMode, int BMode, int Prec, bool kReal>
 cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
                          int* err_flag, dim3 tiles) {
+  constexpr int kSmem = smem_bytes_1<kReal>();
+  static_assert(kSmem <= 227 * 1024, "shared memory budget");
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc1m_contract<AMode, BMode, Prec>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemBytes);
+    cudaError_t e = cudaFuncSetAttribute(tc1m_contract<AMode, BMode, Prec, kReal>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  tc1m_contract<AMode, BMode, Prec><<<tiles, kThreads1, kSmemBytes, stream>>>(args, maps, err_flag);
+  tc1m_contract<AMode, BMode, Prec, kReal><<<tiles, kThreads1, kSmem, stream>>>(args, maps,
+                                                                                  err_flag);
   return cudaGetLastError();
 }
 
-template <int AMode, int Prec>
+template <int AMode, int Prec, bool kReal>
 cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
                      int* err_flag, dim3 tiles) {
   switch (bmode) {
-    case kTmaNK: return launch_modes<AMode, kTmaNK, Prec>(args, maps, stream, err_flag, tiles);
-    case kTmaKN: return launch_modes<AMode, kTmaKN, Prec>(args, maps, stream, err_flag, tiles);
-    default: return launch_modes<AMode, kGatherNK, Prec>(args, maps, stream, err_flag, tiles);
+    case kTmaNK: return launch_modes<AMode, kTmaNK, Prec, kReal>(args, maps, stream, err_flag, tiles);
+    case kTmaKN: return launch_modes<AMode, kTmaKN, Prec, kReal>(args, maps, stream, err_flag, tiles);
+    default: return launch_modes<AMode, kGatherNK, Prec, kReal>(args, maps, stream, err_flag, tiles);
   }
 }
 
-template <int Prec>
+template <int Prec, bool kReal>
 cudaError_t launch_a(int amode, int bmode, const GemmArgs& args, const TmaMaps& maps,
                      cudaStream_t stream, int* err_flag, dim3 tiles) {
   switch (amode) {
-    case kTmaMK: return launch_b<kTmaMK, Prec>(bmode, args, maps, stream, err_flag, tiles);
-    case kTmaKM: return launch_b<kTmaKM, Prec>(bmode, args, maps, stream, err_flag, tiles);
-    default: return launch_b<kGatherMK, Prec>(bmode, args, maps, stream, err_flag, tiles);
+    case kTmaMK: return launch_b<kTmaMK, Prec, kReal>(bmode, args, maps, stream, err_flag, tiles);
+    case kTmaKM: return launch_b<kTmaKM, Prec, kReal>(bmode, args, maps, stream, err_flag, tiles);
+    default: return launch_b<kGatherMK, Prec, kReal>(bmode, args, maps, stream, err_flag, tiles);
   }
 }
+
+template <bool kReal>
+cudaError_t launch_prec(int method, int amode, int bmode, const GemmArgs& args,
+                        const TmaMaps& maps, cudaStream_t stream, int* err_flag, dim3 tiles) {
+  switch (method) {
+    case T1M_METHOD_TC_BF16X3:
+      return launch_a<kPrecBF16x3, kReal>(amode, bmode, args, maps, stream, err_flag, tiles);
+    case T1M_METHOD_TC_BF16X6:
+      return launch_a<kPrecBF16x6, kReal>(amode, bmode, args, maps, stream, err_flag, tiles);
+    default:
+      return launch_a<kPrecTF32x3, kReal>(amode, bmode, args, maps, stream, err_flag, tiles);
+  }
+}
+
+// 2-D map over float32 data: dim0 = inner floats (unit stride), dim1 =
+// outer with `outer_stride` floats.
+bool make_map_f32(CUtensorMap* map, const void* base, int64_t inner, int64_t outer,
+                  int64_t outer_stride, uint32_t box_inner, uint32_t box_outer, bool swizzle);
+
+// Real float32 problems on the one-tile kernel: uniform-view TMA modes or
+// gathers (no per-block maps), epilogue flags for 4-column stores.
+bool tc_prepare_real(const GemmArgs& g, const HostPlan& plan, int splits, int* amode,
+                     int* bmode, TmaMaps* maps, GemmArgs* out);
 
 // Rows of every 16-aligned block of `rows` step by one common stride *stride
 // (the same for all blocks, a 16-byte multiple), and every block start plus
@@ -1539,22 +1757,107 @@ uint32_t c_store_flags(const GemmArgs& g, const HostPlan& plan) {
   return f;
 }
 
+bool make_map_f32(CUtensorMap* map, const void* base, int64_t inner, int64_t outer,
+                  int64_t outer_stride, uint32_t box_inner, uint32_t box_outer, bool swizzle) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  if (reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  if (outer > 1 && ((outer_stride * 4) % 16 != 0 || outer_stride <= 0)) return false;
+  if (inner >= (int64_t(1) << 31) || outer >= (int64_t(1) << 31) || inner <= 0 || outer <= 0)
+    return false;
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(inner), static_cast<cuuint64_t>(outer)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(outer > 1 ? outer_stride * 4 : 16)};
+  cuuint32_t box[2] = {box_inner, box_outer};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+// Real epilogue flags: kFlagCCol16 as for complex; kFlagCPairs for four
+// consecutive columns contiguous with 16-byte aligned starts.
+uint32_t c_store_flags_real(const GemmArgs& g, const HostPlan& plan) {
+  auto col = [&](int64_t n) { return g.uC_n >= 0 ? n * g.uC_n : plan.csC[n]; };
+  auto row = [&](int64_t m) { return g.uC_m >= 0 ? m * g.uC_m : plan.rsC[m]; };
+  uint32_t f = 0;
+  bool col16 = true;
+  if (g.uC_n >= 0) {
+    col16 = g.uC_n == 1 || g.N <= 1;
+  } else {
+    for (int64_t b = 0; b < g.N && col16; b += 16)
+      for (int64_t i = b + 1; i < std::min<int64_t>(g.N, b + 16); ++i)
+        if (col(i) != col(b) + (i - b)) {
+          col16 = false;
+          break;
+        }
+  }
+  if (col16) f |= kFlagCCol16;
+  bool quads = reinterpret_cast<uintptr_t>(g.C) % 16 == 0;
+  if (quads) {
+    if (g.uC_m >= 0) {
+      quads = g.uC_m % 4 == 0 || g.M <= 1;
+    } else {
+      for (int64_t m = 0; m < g.M && quads; ++m) quads = row(m) % 4 == 0;
+    }
+  }
+  if (quads) {
+    if (g.uC_n >= 0) {
+      quads = g.uC_n == 1;
+    } else {
+      for (int64_t n = 0; n + 3 < g.N && quads; n += 4)
+        quads = col(n) % 4 == 0 && col(n + 1) == col(n) + 1 && col(n + 2) == col(n) + 2 &&
+                col(n + 3) == col(n) + 3;
+    }
+  }
+  if (quads) f |= kFlagCPairs;
+  return f;
+}
+
+bool tc_prepare_real(const GemmArgs& g, const HostPlan& plan, int splits, int* amode,
+                     int* bmode, TmaMaps* maps, GemmArgs* out) {
+  constexpr int kStepKR = 32;
+  if (splits < 1 || (splits > 1 && g.k_per_split % kStepKR != 0)) return false;
+  if (g.M >= (int64_t(1) << 31) / 128 || g.N >= (int64_t(1) << 31) / kTileN) return false;
+  *out = g;
+  out->flags = (g.flags & ~(kFlagCPairs | kFlagCCol16 | kFlagConjA | kFlagConjB)) |
+               c_store_flags_real(g, plan);
+  std::memset(static_cast<void*>(maps), 0, sizeof(*maps));
+  *amode = kGatherMK;
+  if (plan.uA_m == 1 && plan.uA_k >= 0 &&
+      make_map_f32(&maps->a, g.A, g.M, g.K, plan.uA_k, 128, kStepKR, false))
+    *amode = kTmaMK;
+  else if (plan.uA_k == 1 && plan.uA_m >= 0 &&
+           make_map_f32(&maps->a, g.A, g.K, g.M, plan.uA_m, kStepKR, 128, true))
+    *amode = kTmaKM;
+  *bmode = kGatherNK;
+  if (plan.uB_k == 1 && plan.uB_n >= 0 &&
+      make_map_f32(&maps->b, g.B, g.K, g.N, plan.uB_n, kStepKR, kTileN, true))
+    *bmode = kTmaNK;
+  else if (plan.uB_n == 1 && plan.uB_k >= 0 &&
+           make_map_f32(&maps->b, g.B, g.N, g.K, plan.uB_k, kTileN, kStepKR, false))
+    *bmode = kTmaKN;
+  return true;
+}
+
 std::mutex g_attr_mutex;
 bool g_attr_set = false;
 
 }  // namespace
 
-void tc_tile(int* bm, int* bn, int* bk) {
-  *bm = kTileMc;
+void tc_tile(int dtype, int* bm, int* bn, int* bk) {
+  const bool real = dtype == T1M_FLOAT32;
+  *bm = real ? 128 : kTileMc;
   *bn = kTileN;
-  *bk = kStepK;
+  *bk = real ? 32 : kStepK;
 }
 
 bool tc_supported(int method, int dtype, const HostPlan& plan) {
   (void)plan;
   return (method == T1M_METHOD_TC_3XTF32 || method == T1M_METHOD_TC_BF16X3 ||
           method == T1M_METHOD_TC_BF16X6 || method == kMethodTcAuto) &&
-         dtype == T1M_COMPLEX64;
+         (dtype == T1M_COMPLEX64 || dtype == T1M_FLOAT32);
 }
 
 bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p) {
@@ -1665,6 +1968,22 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     return cudaErrorNotSupported;
   }
   if (args.M == 0 || args.N == 0) return cudaSuccess;
+  if (dtype == T1M_FLOAT32) {
+    // Real float32: the one-tile kernel with uniform-view TMA or gathers.
+    int am = kGatherMK, bm = kGatherNK;
+    TmaMaps maps;
+    GemmArgs gr;
+    if (!tc_prepare_real(args, plan, splits, &am, &bm, &maps, &gr))
+      return cudaErrorInvalidConfiguration;
+    if (method == kMethodTcAuto)
+      method = (am != kGatherMK && bm != kGatherNK) ? T1M_METHOD_TC_BF16X6 : T1M_METHOD_TC_3XTF32;
+    if (used_method) *used_method = method;
+    const dim3 grid(static_cast<unsigned>(((args.M + 127) / 128) * ((args.N + kTileN - 1) / kTileN)),
+                    static_cast<unsigned>(splits));
+    const cudaError_t e = launch_prec<true>(method, am, bm, gr, maps, stream, err_flag, grid);
+    if (e == cudaSuccess) *kernels = 1;
+    return e;
+  }
   TcProblem p;
   if (!tc_prepare(args, plan, splits, &p)) return cudaErrorInvalidConfiguration;
   p.tile_begin = 0;
@@ -1698,15 +2017,7 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                    : (a_uniform && p.amode == kAKM) ? kTmaKM : kGatherMK;
     const int bm = (b_uniform && p.bmode == kBNK) ? kTmaNK
                    : (b_uniform && p.bmode == kBKN) ? kTmaKN : kGatherNK;
-    switch (method) {
-      case T1M_METHOD_TC_BF16X3:
-        e = launch_a<kPrecBF16x3>(am, bm, p.g, maps, stream, err_flag, grid);
-        break;
-      case T1M_METHOD_TC_BF16X6:
-        e = launch_a<kPrecBF16x6>(am, bm, p.g, maps, stream, err_flag, grid);
-        break;
-      default: e = launch_a<kPrecTF32x3>(am, bm, p.g, maps, stream, err_flag, grid); break;
-    }
+    e = launch_prec<false>(method, am, bm, p.g, maps, stream, err_flag, grid);
   } else {
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
   }
