@@ -1254,8 +1254,9 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
                     : cudaErrorInvalidValue;
           } else if (f == kFamSimtSkinny) {
             SimtProblem sp{probe, 0};
-            cudaMemcpy(pd, &sp, sizeof(sp), cudaMemcpyHostToDevice);
             const int nmax = hp.N <= 4 ? 4 : 16;
+            if (skinny_async_ok(sp.g, hp.rsA, es, nmax)) sp.g.flags |= kFlagSkinnyAsync;
+            cudaMemcpy(pd, &sp, sizeof(sp), cudaMemcpyHostToDevice);
             le = launch_skinny_group(dtype, nmax, static_cast<SimtProblem*>(pd), 1,
                                      skinny_tiles(probe, nsp, nmax), ctx->stream);
           } else {
@@ -1367,6 +1368,7 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
           tcs.push_back(tp);
         } else if (fam == kFamSimtSkinny) {
           SimtProblem sp{main_args[i], L.tiles};
+          if (skinny_async_ok(sp.g, hp.rsA, es, L.nmax)) sp.g.flags |= kFlagSkinnyAsync;
           L.tiles += skinny_tiles(main_args[i], splits[i], L.nmax);
           simts.push_back(sp);
         } else {

@@ -105,6 +105,11 @@ constexpr uint32_t kFlagBetaZero = 16u;  // BLAS semantics with beta == 0
 // every 16-column block (one offset lookup per 16 columns).
 constexpr uint32_t kFlagCPairs = 32u;
 constexpr uint32_t kFlagCCol16 = 64u;
+// Skinny kernel: A streams through a cp.async shared-memory pipeline (set by
+// the host where A has unit K stride, 8-byte elements, 16-byte aligned rows,
+// a K chunk of at most kSkinnyAsyncMaxK and N <= 4).
+constexpr uint32_t kFlagSkinnyAsync = 128u;
+constexpr int kSkinnyAsyncMaxK = 1024;
 
 // Internal method id: tensor cores, precision chosen per problem by the
 // launcher (BF16x6 where the one-tile kernel fetches both operands by TMA,
@@ -139,6 +144,9 @@ constexpr int kSkinnyMaxN = 16;
 __host__ __device__ constexpr int skinny_rows(bool k_unit, int nmax) {
   return k_unit ? 8 * (16 / nmax) : 256;
 }
+// kFlagSkinnyAsync for an item of a skinny launch of column bound nmax
+// (rs: the plan's A row offsets; uniform stride uA_m where >= 0).
+bool skinny_async_ok(const GemmArgs& g, const std::vector<int64_t>& rsA, size_t elem, int nmax);
 // Tiles of one skinny problem: splits x ceil(M / rows).
 int64_t skinny_tiles(const GemmArgs& g, int splits, int nmax);
 cudaError_t launch_skinny_group(int dtype, int nmax, const SimtProblem* dev, int nprob,

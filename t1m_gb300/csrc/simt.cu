@@ -10,7 +10,9 @@
 // C += alpha*A*B under kFlagAccumulate, t1m.h:406-430).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
+#include <vector>
 
 #include "internal.h"
 
@@ -438,12 +440,138 @@ __device__ __forceinline__ void skinny_body(const GemmArgs& g, int64_t tile, T (
   }
 }
 
+// Asynchronous form (kFlagSkinnyAsync, N <= 4, 8-byte elements, unit K
+// stride): the CTA's 32 rows stream through a ring of kSkStages shared-memory
+// stages of 64 k with cp.async (16 bytes per copy, zero fill past the edges),
+// so the loads in flight no longer depend on registers; B's whole K chunk
+// (at most kSkinnyAsyncMaxK) is staged once.  Warp w reduces rows 4w..4w+3,
+// lanes over k as in skinny_body.
+constexpr int kSkStages = 3;
+constexpr int kSkKS = 64;  // k per stage
+constexpr size_t kSkAsyncSmem =
+    size_t(kSkStages) * 32 * kSkKS * 8 + size_t(4) * kSkinnyAsyncMaxK * 8;  // 80 KB
+
+__device__ __forceinline__ void cp_async_16(uint32_t dst, const void* src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
+               "r"(src_bytes)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+template <class T>
+__device__ __forceinline__ void skinny_async_body(const GemmArgs& g, int64_t tile,
+                                                  unsigned char* dsmem) {
+  static_assert(sizeof(T) == 8, "8-byte elements");
+  constexpr int NMAX = 4, RW = 4;
+  T (*ring)[32][kSkKS] = reinterpret_cast<T (*)[32][kSkKS]>(dsmem);
+  T (*Bs)[kSkinnyAsyncMaxK] =
+      reinterpret_cast<T (*)[kSkinnyAsyncMaxK]>(dsmem + size_t(kSkStages) * 32 * kSkKS * 8);
+  const int64_t M = g.M, N = g.N, K = g.K;
+  const int64_t tiles_m = (M + 31) / 32;
+  const int64_t split = tile / tiles_m;
+  const int64_t m0 = (tile - split * tiles_m) * 32;
+  const int64_t kb = split * g.k_per_split;
+  const int64_t ke = min(K, kb + g.k_per_split);
+  const int kn = static_cast<int>(ke - kb);
+  const int nst = (kn + kSkKS - 1) / kSkKS;
+  T* __restrict__ C = static_cast<T*>(g.C) + split * g.c_split_stride;
+  const T* __restrict__ A = static_cast<const T*>(g.A);
+  const T* __restrict__ B = static_cast<const T*>(g.B);
+  const bool conjA = g.flags & kFlagConjA;
+  const bool conjB = g.flags & kFlagConjB;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  // B chunk, zero-padded to NMAX columns and to whole stages.
+  for (int e = tid; e < NMAX * nst * kSkKS; e += kThreads) {
+    const int n = e / (nst * kSkKS), kk = e % (nst * kSkKS);
+    T v = zero<T>();
+    if (n < N && kk < kn)
+      v = conj_if(B[offs(g.rsB, g.uB_k, kb + kk) + offs(g.csB, g.uB_n, n)], conjB);
+    Bs[n][kk] = v;
+  }
+  // Copies of this thread: 16-byte chunk c = tid + 256 i of a stage, row
+  // c / 32, elements 2 (c % 32) and 2 (c % 32) + 1.
+  int64_t rowoff[4];
+  bool rok[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = (tid >> 5) + 8 * i;
+    rok[i] = m0 + r < M;
+    rowoff[i] = rok[i] ? offs(g.rsA, g.uA_m, m0 + r) : 0;
+  }
+  const int kk2 = 2 * (tid & 31);
+  auto issue = [&](int s) {
+    const int slot = s % kSkStages;
+    const int64_t k0 = kb + int64_t(s) * kSkKS;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = (tid >> 5) + 8 * i;
+      const int64_t k = k0 + kk2;
+      const bool in = rok[i] && k < ke;
+      const uint32_t bytes = in ? static_cast<uint32_t>(min(static_cast<int64_t>(2), ke - k) * 8) : 0u;
+      const T* src = in ? A + rowoff[i] + k : A;
+      cp_async_16(static_cast<uint32_t>(__cvta_generic_to_shared(&ring[slot][r][kk2])), src, bytes);
+    }
+    cp_async_commit();
+  };
+#pragma unroll
+  for (int s = 0; s < kSkStages - 1; ++s) {
+    if (s < nst) issue(s);
+    else cp_async_commit();
+  }
+  T acc[RW][NMAX];
+#pragma unroll
+  for (int r = 0; r < RW; ++r)
+#pragma unroll
+    for (int n = 0; n < NMAX; ++n) acc[r][n] = zero<T>();
+  for (int s = 0; s < nst; ++s) {
+    cp_async_wait<kSkStages - 2>();
+    __syncthreads();  // stage s visible to all; the slot refilled below is free
+    const int slot = s % kSkStages;
+#pragma unroll
+    for (int u = 0; u < kSkKS / 32; ++u) {
+      const int kk = lane + 32 * u;
+#pragma unroll
+      for (int r = 0; r < RW; ++r) {
+        const T a = conj_if(ring[slot][warp * RW + r][kk], conjA);
+#pragma unroll
+        for (int n = 0; n < NMAX; ++n) mac(acc[r][n], a, Bs[n][s * kSkKS + kk]);
+      }
+    }
+    if (s + kSkStages - 1 < nst) issue(s + kSkStages - 1);
+    else cp_async_commit();
+  }
+  cp_async_wait<0>();
+#pragma unroll
+  for (int r = 0; r < RW; ++r) {
+#pragma unroll
+    for (int n = 0; n < NMAX; ++n) {
+      T v = acc[r][n];
+#pragma unroll
+      for (int d = 16; d >= 1; d >>= 1) v = add(v, shfl_xor(v, d));
+      acc[r][n] = v;
+    }
+    const int64_t m = m0 + warp * RW + r;
+    if (lane == 0 && m < M)
+#pragma unroll
+      for (int n = 0; n < NMAX; ++n)
+        if (n < N) skinny_store(g, C, m, n, acc[r][n]);
+  }
+}
+
 template <class T, int NMAX>
 __global__ void __launch_bounds__(kThreads)
 skinny_contract(const SimtProblem* group, int nprob) {
   __shared__ GemmArgs ga;
   __shared__ __align__(16) T Bs[NMAX][2048 / NMAX];
   __shared__ int64_t ks[2048 / NMAX];
+  extern __shared__ __align__(16) unsigned char skinny_dsmem[];
   int64_t tile = blockIdx.x;
   int lo = 0, hi = nprob - 1;
   while (lo < hi) {
@@ -453,6 +581,12 @@ skinny_contract(const SimtProblem* group, int nprob) {
   tile -= group[lo].tile_begin;
   if (threadIdx.x == 0) ga = group[lo].g;
   __syncthreads();
+  if constexpr (NMAX == 4 && sizeof(T) == 8) {
+    if (ga.flags & kFlagSkinnyAsync) {
+      skinny_async_body<T>(ga, tile, skinny_dsmem);
+      return;
+    }
+  }
   if (ga.uA_k == 1)
     skinny_body<T, NMAX, true>(ga, tile, Bs, ks);
   else
@@ -464,8 +598,20 @@ cudaError_t launch_skinny(const SimtProblem* dev, int nprob, int64_t total_tiles
                           cudaStream_t stream) {
   if (total_tiles <= 0) return cudaSuccess;
   if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  skinny_contract<T, NMAX><<<static_cast<unsigned>(total_tiles), kThreads, 0, stream>>>(dev,
-                                                                                       nprob);
+  // The asynchronous form's ring and B chunk (dynamic shared memory) exist
+  // only in the instances that can run it.
+  constexpr size_t kDyn = (NMAX == 4 && sizeof(T) == 8) ? kSkAsyncSmem : 0;
+  if constexpr (kDyn > 0) {
+    static bool attr_set = false;
+    if (!attr_set) {
+      const cudaError_t e = cudaFuncSetAttribute(
+          skinny_contract<T, NMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kDyn));
+      if (e != cudaSuccess) return e;
+      attr_set = true;
+    }
+  }
+  skinny_contract<T, NMAX><<<static_cast<unsigned>(total_tiles), kThreads, kDyn, stream>>>(
+      dev, nprob);
   return cudaGetLastError();
 }
 
@@ -482,6 +628,17 @@ cudaError_t launch_skinny_dtype(int dtype, const SimtProblem* dev, int nprob, in
 }
 
 }  // namespace
+
+bool skinny_async_ok(const GemmArgs& g, const std::vector<int64_t>& rsA, size_t elem, int nmax) {
+  if (nmax != 4 || elem != 8 || g.uA_k != 1 || g.N > 4) return false;
+  if (reinterpret_cast<uintptr_t>(g.A) % 16 != 0) return false;
+  if (std::min<int64_t>(g.K, g.k_per_split) > kSkinnyAsyncMaxK) return false;
+  if (g.k_per_split % 2 != 0 && g.k_per_split < g.K) return false;  // split starts stay even
+  if (g.uA_m >= 0) return g.uA_m % 2 == 0 || g.M <= 1;
+  for (int64_t m = 0; m < g.M; ++m)
+    if (rsA[m] % 2 != 0) return false;
+  return true;
+}
 
 int64_t skinny_tiles(const GemmArgs& g, int splits, int nmax) {
   const int64_t rows = skinny_rows(g.uA_k == 1, nmax);
