@@ -803,11 +803,11 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
     float master[64];
     auto fold_from = [&](uint32_t col) {
 #pragma unroll
-      for (int cc = 0; cc < 4; ++cc) {
-        uint32_t r[16];
-        ptx::tmem_ld16_sync(tmem + lane_base + col + 64u * wg + 16u * cc, r);
+      for (int cc = 0; cc < 2; ++cc) {
+        uint32_t r[32];
+        ptx::tmem_ld32_sync(tmem + lane_base + col + 64u * wg + 32u * cc, r);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) master[16 * cc + j] += __uint_as_float(r[j]);
+        for (int j = 0; j < 32; ++j) master[32 * cc + j] += __uint_as_float(r[j]);
       }
     };
 
@@ -1075,7 +1075,7 @@ constexpr int kAK1 = kStepK / kCW1;                          // complex k of A p
 constexpr int kMC1 = kTileN / kCW1;                          // accumulator columns per thread
 constexpr int kBP1 = (kTileN * kStepK / 2) / kConverters1;   // 16-byte B pieces per thread
 constexpr int kB16P1 = (kTileN * kStepK / 4) / kConverters1; // bf16 B chunks per thread
-static_assert(kAK1 % 4 == 0 && kMC1 % 16 == 0 && kBP1 >= 1 && kB16P1 >= 1, "converter split");
+static_assert(kAK1 % 4 == 0 && kMC1 % 32 == 0 && kBP1 >= 1 && kB16P1 >= 1, "converter split");
 
 // Real float32 (kReal): the same GEMM without the 1M expansion.  A tile is
 // 128 real rows (one TMEM lane each), K is staged 32 reals per stage (the
@@ -1300,11 +1300,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     // (round-to-nearest adds): this thread's lane, kMC1 columns.
     auto fold_from = [&](uint32_t col) {
 #pragma unroll
-      for (int cc = 0; cc < kMC1 / 16; ++cc) {
-        uint32_t r[16];
-        ptx::tmem_ld16_sync(tmem + lane_base + col + kMC1 * wg + 16u * cc, r);
+      for (int cc = 0; cc < kMC1 / 32; ++cc) {
+        uint32_t r[32];
+        ptx::tmem_ld32_sync(tmem + lane_base + col + kMC1 * wg + 32u * cc, r);
 #pragma unroll
-        for (int j = 0; j < 16; ++j) master[16 * cc + j] += __uint_as_float(r[j]);
+        for (int j = 0; j < 32; ++j) master[32 * cc + j] += __uint_as_float(r[j]);
       }
     };
 
