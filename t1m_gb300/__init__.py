@@ -200,18 +200,32 @@ def default_context() -> Context:
     return _default_ctx
 
 
+_TORCH_NP: dict | None = None
+
+
+def _torch_dtypes() -> dict:
+    """torch element type -> numpy dtype, built on first use (torch is
+    plumbing for device memory only and need not be installed)."""
+    global _TORCH_NP
+    if _TORCH_NP is None:
+        try:
+            import torch
+            _TORCH_NP = {torch.float32: np.dtype(np.float32), torch.float64: np.dtype(np.float64),
+                         torch.complex64: np.dtype(np.complex64),
+                         torch.complex128: np.dtype(np.complex128)}
+        except ImportError:
+            _TORCH_NP = {}
+    return _TORCH_NP
+
+
 def _data_ptr(data: Any) -> tuple[int, np.dtype]:
     if isinstance(data, np.ndarray):
         return data.ctypes.data, data.dtype
-    try:
-        import torch  # plumbing only: device memory
-        if isinstance(data, torch.Tensor):
-            npdt = {torch.float32: np.float32, torch.float64: np.float64,
-                    torch.complex64: np.complex64, torch.complex128: np.complex128}[data.dtype]
-            return data.data_ptr(), np.dtype(npdt)
-    except ImportError:
-        pass
-    raise TypeError(f"unsupported tensor storage {type(data)!r}")
+    npdt = _torch_dtypes().get(getattr(data, "dtype", None))
+    if npdt is not None and hasattr(data, "data_ptr"):
+        return data.data_ptr(), npdt
+    raise TypeError(f"unsupported tensor storage {type(data)!r} "
+                    f"(element type {getattr(data, 'dtype', None)})")
 
 
 @dataclass
@@ -232,8 +246,9 @@ class tensor:
     def dtype(self) -> np.dtype:
         return _data_ptr(self.data)[1]
 
-    def _c(self, keep: list) -> _Tensor:
-        ptr, _ = _data_ptr(self.data)
+    def _c(self, keep: list, ptr: int | None = None) -> _Tensor:
+        if ptr is None:
+            ptr = _data_ptr(self.data)[0]
         ext = (C.c_int64 * max(1, len(self.dims)))(*[int(d) for d in self.dims])
         keep.append(ext)
         t = _Tensor(len(self.dims), int(self.layout), ext, None, ptr)
@@ -266,17 +281,16 @@ def contract_raw(alpha, a: tensor, la: str, b: tensor, lb: str, beta, c: tensor,
                  flags: int = 0, ctx: Context | None = None) -> Report:
     """One call of t1m_contract; returns its report."""
     ctx = ctx or default_context()
-    dts = {a.dtype(), b.dtype(), c.dtype()}
-    if len(dts) != 1:
-        raise TypeError(f"mixed element types {dts}")
-    dtype = _DTYPE_OF[dts.pop()]
+    (pa, da), (pb, db), (pc, dc) = _data_ptr(a.data), _data_ptr(b.data), _data_ptr(c.data)
+    if not da == db == dc:
+        raise TypeError(f"mixed element types {(str(da), str(db), str(dc))}")
+    dtype = _DTYPE_OF[da]
     keep: list = []
-    ta, tb, tc = a._c(keep), b._c(keep), c._c(keep)
+    ta, tb, tc = a._c(keep, pa), b._c(keep, pb), c._c(keep, pc)
     al, be = _scalar_bytes(dtype, alpha), _scalar_bytes(dtype, beta)
     rep = Report()
-    st = lib().t1m_contract(ctx.handle, dtype, C.cast(al, C.c_void_p), C.byref(ta),
-                            la.encode(), C.byref(tb), lb.encode(), C.cast(be, C.c_void_p),
-                            C.byref(tc), lc.encode(), int(flags), C.byref(rep))
+    st = lib().t1m_contract(ctx.handle, dtype, al, C.byref(ta), la.encode(), C.byref(tb),
+                            lb.encode(), be, C.byref(tc), lc.encode(), int(flags), C.byref(rep))
     if st != OK:
         raise T1MError(st, (lib().t1m_last_error(ctx.handle) or b"").decode())
     return rep
