@@ -108,7 +108,9 @@ typedef struct t1m_context t1m_context;
  * handle: stream, method and plan cache). */
 int t1m_create(t1m_context** ctx, int device);
 int t1m_destroy(t1m_context* ctx);
-/* Run on a caller-owned cudaStream_t (NULL = the context's own stream). */
+/* Run on a caller-owned cudaStream_t (NULL = the context's own stream).
+ * Switching waits for the work queued on the previous stream (the context's
+ * workspaces are shared by its calls). */
 int t1m_set_stream(t1m_context* ctx, void* stream);
 int t1m_set_method(t1m_context* ctx, int method);
 /* Number of K partitions (split-K with an FP64 reduction of the partial

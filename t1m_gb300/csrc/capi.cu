@@ -27,11 +27,6 @@ using namespace t1m::gb300;
 
 namespace t1m {
 namespace gb300 {
-cudaError_t launch_tc(int method, int dtype, const GemmArgs& args,
-                      const HostPlan& plan, int splits, cudaStream_t stream,
-                      int* err_flag, int* kernels, std::string* err, int* used_method);
-bool tc_supported(int method, int dtype, const HostPlan& plan);
-void tc_tile(int dtype, int* bm, int* bn, int* bk);
 cudaError_t launch_dmma(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
                         int* kernels);
 void dmma_tile(int* bm, int* bn, int* bk);
@@ -61,6 +56,9 @@ struct t1m_context {
   // Split-K workspace (grow only) and the forced split count (0 = automatic).
   void* work = nullptr;
   size_t work_bytes = 0;
+  // B-panel workspace of the tensor-core kernels (grow only).
+  void* panel = nullptr;
+  size_t panel_bytes = 0;
   int split_k = 0;
   int num_sms = 152;
   // Host-operand pipeline: copy-in and copy-out streams beside the compute
@@ -251,6 +249,25 @@ int ensure_work(t1m_context* ctx, size_t bytes) {
   return T1M_OK;
 }
 
+// B-panel workspace: the panels are an optimisation, so a failed allocation
+// leaves the product on the converter path instead of failing it.
+bool ensure_panel(t1m_context* ctx, size_t bytes) {
+  if (ctx->panel_bytes >= bytes) return true;
+  if (ctx->panel) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->panel);
+  }
+  ctx->panel = nullptr;
+  ctx->panel_bytes = 0;
+  if (cudaMalloc(&ctx->panel, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    ctx->panel = nullptr;
+    return false;
+  }
+  ctx->panel_bytes = bytes;
+  return true;
+}
+
 // One product C = alpha*A*B (+ beta*C) on stream s, its operands already in
 // g (shifted for a batch index or a slab): method checks, split-K (raw
 // partials in the workspace, FP64 reduction with the epilogue) and the
@@ -300,7 +317,10 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
     } else {
       std::string err;
       int ran = method;
-      e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran);
+      const size_t pb = tc_panel_bytes(dtype, gm.M, gm.N, gm.K);
+      const bool pan = pb > 0 && ensure_panel(ctx, pb);
+      e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
+                    pan ? ctx->panel : nullptr, pan ? ctx->panel_bytes : 0);
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -570,6 +590,7 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->work) cudaFree(ctx->work);
+  if (ctx->panel) cudaFree(ctx->panel);
   for (int i = 0; i < t1m_context::kPipeEvents; ++i)
     if (ctx->pev[i]) cudaEventDestroy(ctx->pev[i]);
   if (ctx->copy_in) {
@@ -587,7 +608,15 @@ int t1m_destroy(t1m_context* ctx) {
 
 int t1m_set_stream(t1m_context* ctx, void* stream) {
   if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
-  ctx->stream = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  const cudaStream_t next = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  // The context's workspaces (split-K partials, B panels) are reused by every
+  // call: work queued on the previous stream finishes before the switch.
+  if (next != ctx->stream && ctx->stream) {
+    cudaSetDevice(ctx->device);
+    const cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "drain the previous stream");
+  }
+  ctx->stream = next;
   return T1M_OK;
 }
 

@@ -169,5 +169,17 @@ struct SplitReduce {
 cudaError_t launch_splitk_reduce_group(int dtype, const SplitReduce* dev, int n,
                                        int64_t total, cudaStream_t stream);
 
+// tc.cu: one contraction on the tensor cores (complex64 / float32, split
+// methods).  `panel` (panel_bytes) is workspace for B split once into
+// panels, at least tc_panel_bytes(dtype, M, N, K) bytes, or null.
+cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
+                      int splits, cudaStream_t stream, int* err_flag, int* kernels,
+                      std::string* err, int* used_method, void* panel = nullptr,
+                      size_t panel_bytes = 0);
+// Panel workspace a product would use (0: panels not used at this size).
+size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K);
+bool tc_supported(int method, int dtype, const HostPlan& plan);
+void tc_tile(int dtype, int* bm, int* bn, int* bk);
+
 }  // namespace gb300
 }  // namespace t1m

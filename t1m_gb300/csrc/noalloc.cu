@@ -37,11 +37,6 @@
 
 namespace t1m {
 namespace gb300 {
-cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
-                      int splits, cudaStream_t stream, int* err_flag, int* kernels,
-                      std::string* err, int* used_method);
-bool tc_supported(int method, int dtype, const HostPlan& plan);
-void tc_tile(int dtype, int* bm, int* bn, int* bk);
 cudaError_t launch_dmma(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
                         int* kernels);
 void dmma_tile(int* bm, int* bn, int* bk);

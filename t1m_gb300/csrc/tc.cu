@@ -1043,6 +1043,75 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
   }
 }
 
+// ---------------------------------------------------------- B panels ---
+// B split once for all M tiles: row n of the panel array holds, per stage of
+// 32 real k (16 complex k), kBufs rows of 128 bytes, the bytes the converters
+// would write into the operand stage for column n before the 128-byte swizzle
+// (which the TMA load of a panel stage applies):
+//   3xTF32: [hi of the 32 values] [lo]
+//   BF16x3: [piece 0 (32 bf16) | piece 1]
+//   BF16x6: [piece 0 | piece 1] [piece 2 | zeros]
+// Values in k order: re, im (conjugated under kFlagConjB) of each complex k,
+// or the real k; zero past K.  The pieces are the converters' (same split
+// functions), so a product is bit-identical with or without panels.
+// One thread per (column, stage); stages fastest when B has unit K stride
+// (contiguous reads and writes), columns fastest otherwise (reads coalesced
+// across columns).
+template <int Prec, bool kReal>
+__global__ void __launch_bounds__(256)
+split_b_panels(const GemmArgs g, uint4* __restrict__ out, int64_t nstages, int k_fastest) {
+  constexpr int kBufs = Prec == kPrecBF16x3 ? 1 : 2;
+  const int64_t idx = static_cast<int64_t>(blockIdx.x) * 256 + threadIdx.x;
+  if (idx >= g.N * nstages) return;
+  const int64_t n = k_fastest ? idx / nstages : idx % g.N;
+  const int64_t s = k_fastest ? idx % nstages : idx / g.N;
+  const int64_t cn = offs(g.csB, g.uB_n, n);
+  float v[32];
+  if constexpr (kReal) {
+    const float* __restrict__ B = static_cast<const float*>(g.B);
+#pragma unroll
+    for (int j = 0; j < 32; ++j) {
+      const int64_t k = 32 * s + j;
+      v[j] = k < g.K ? B[cn + offs(g.rsB, g.uB_k, k)] : 0.f;
+    }
+  } else {
+    const float2* __restrict__ B = static_cast<const float2*>(g.B);
+    const bool conj = g.flags & kFlagConjB;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int64_t k = 16 * s + j;
+      const float2 x = k < g.K ? B[cn + offs(g.rsB, g.uB_k, k)] : make_float2(0.f, 0.f);
+      v[2 * j] = x.x;
+      v[2 * j + 1] = conj ? -x.y : x.y;
+    }
+  }
+  uint4* __restrict__ row = out + (n * nstages + s) * (8 * kBufs);
+  if constexpr (Prec == kPrecTF32x3) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const Split a = split_tf32(v[4 * q]), b = split_tf32(v[4 * q + 1]);
+      const Split c = split_tf32(v[4 * q + 2]), d = split_tf32(v[4 * q + 3]);
+      row[q] = make_uint4(a.hi, b.hi, c.hi, d.hi);
+      row[8 + q] = make_uint4(a.lo, b.lo, c.lo, d.lo);
+    }
+  } else {
+    constexpr int kPieces = Prec == kPrecBF16x6 ? 3 : 2;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      uint32_t w[4][3];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        split_bf16<kPieces>(v[8 * q + 2 * i], v[8 * q + 2 * i + 1], w[i][0], w[i][1], w[i][2]);
+      row[q] = make_uint4(w[0][0], w[1][0], w[2][0], w[3][0]);
+      row[4 + q] = make_uint4(w[0][1], w[1][1], w[2][1], w[3][1]);
+      if (kPieces == 3) {
+        row[8 + q] = make_uint4(w[0][2], w[1][2], w[2][2], w[3][2]);
+        row[12 + q] = make_uint4(0u, 0u, 0u, 0u);
+      }
+    }
+  }
+}
+
 // --------------------------------------------- one tile per CTA variant ---
 // For a single contraction whose operands are a uniform 2-D view or gathered,
 // this non-persistent form (one output tile per CTA, operand modes as template
@@ -1051,7 +1120,13 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
 // fetch modes allow; the persistent kernel serves grouped launches and the
 // per-16-row block TMA modes.
 enum : int { kTmaMK = 0, kTmaKM = 1, kGatherMK = 2 };
-enum : int { kTmaNK = 0, kTmaKN = 1, kGatherNK = 2 };
+// B modes: raw tiles by TMA ([n][k] or [k][n]) or gathered, each split by the
+// converters; or kPanelNK, B split once beforehand into panels
+// (split_b_panels) whose stages TMA loads straight into the operand ring.
+enum : int { kTmaNK = 0, kTmaKN = 1, kGatherNK = 2, kPanelNK = 3 };
+// Operand stages of the panel form: TMA fills them, so the ring is deeper
+// than the converter-written one (which is bounded by the A stages in TMEM).
+constexpr int kPanelStages = 4;
 
 struct TmaMaps {
   CUtensorMap a;
@@ -1082,10 +1157,10 @@ static_assert(kAK1 % 4 == 0 && kMC1 % 32 == 0 && kBP1 >= 1 && kB16P1 >= 1, "conv
 // same 128-byte swizzle rows), the raw A stage doubles to 16 KB, B's raw
 // bytes are the complex layout's (k pairs for complex elements), and the
 // epilogue writes one real row per thread.
-template <bool kReal>
+template <bool kReal, bool kPanel>
 constexpr int smem_bytes_1() {
-  return 1024 + kRaw * ((kReal ? 16384 : kRawABytes) + kRawBBytes) + kStages * kOpBytes +
-         kBarrierBytes;
+  return 1024 + kRaw * ((kReal ? 16384 : kRawABytes) + (kPanel ? 0 : kRawBBytes)) +
+         (kPanel ? kPanelStages : kStages) * kOpBytes + kBarrierBytes;
 }
 
 template <int AMode, int BMode, int Prec, bool kReal>
@@ -1095,13 +1170,16 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   constexpr int kPieces = Prec == kPrecBF16x6 ? 3 : 2;
   constexpr uint32_t kIdescP = kBF16 ? ptx::idesc_f32acc(1u /*BF16*/, 128, kTileN) : kIdesc;
   constexpr bool kTmaA = AMode != kGatherMK;
-  constexpr bool kTmaB = BMode != kGatherNK;
-  constexpr bool kGather = !kTmaA || !kTmaB;
+  constexpr bool kPanel = BMode == kPanelNK;
+  constexpr bool kTmaB = BMode == kTmaNK || BMode == kTmaKN;
+  constexpr bool kGather = !kTmaA || BMode == kGatherNK;
+  constexpr int kOpStages = kPanel ? kPanelStages : kStages;
+  constexpr int kPanelBufs = Prec == kPrecBF16x3 ? 1 : 2;
   constexpr int kRowsT = kReal ? 128 : kTileMc;        // C rows per tile
   constexpr int kStepKE = kReal ? 32 : kStepK;         // K elements per stage
   constexpr int kCx = kReal ? 1 : 2;                   // floats per element (TMA coordinates)
   constexpr int kRawABytesT = kReal ? 16384 : kRawABytes;
-  constexpr int kRawBytesT = kRawABytesT + kRawBBytes;
+  constexpr int kRawBytesT = kRawABytesT + (kPanel ? 0 : kRawBBytes);
   // Arrivals per raw stage: one expect_tx arrive from the TMA thread, one
   // cp.async completion arrive per gather thread.
   constexpr uint32_t kRawArrivals = (kTmaA || kTmaB ? 1u : 0u) + (kGather ? kLoaders : 0u);
@@ -1112,7 +1190,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
   const uint32_t raw0 = base;                          // kRaw x (A | B 16 KB)
   const uint32_t op0 = raw0 + kRaw * kRawBytesT;       // kStages x (B hi | B lo)
-  const uint32_t bars = op0 + kStages * kOpBytes;
+  const uint32_t bars = op0 + kOpStages * kOpBytes;
   auto raw_a = [&](int r) { return raw0 + r * kRawBytesT; };
   auto raw_b = [&](int r) { return raw0 + r * kRawBytesT + kRawABytesT; };
   auto raw_full = [&](int r) { return bars + 8u * r; };
@@ -1123,6 +1201,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   auto chunk_empty = [&](int b) { return bars + 8u * (2 * kRaw + 2 * kStages + 2 + b); };
   const uint32_t acc_bar = bars + 8u * (2 * kRaw + 2 * kStages + 4);
   const uint32_t tmem_slot = acc_bar + 8u;
+  // Panel stages: filled by TMA (one expect_tx arrive), emptied by an MMA commit.
+  auto pfull = [&](int i) { return acc_bar + 16u + 8u * i; };
+  auto pempty = [&](int i) { return acc_bar + 16u + 8u * (kPanelStages + i); };
+  static_assert(8 * (2 * kRaw + 2 * kStages + 5 + 1 + 2 * kPanelStages) <= kBarrierBytes,
+                "barrier area");
   volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(base_ptr + (tmem_slot - base));
 
   const int tid = threadIdx.x;
@@ -1133,6 +1216,12 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     ptx::tmem_relinquish();
   }
   if (tid == 32) {
+    if (kPanel) {
+      for (int i = 0; i < kPanelStages; ++i) {
+        ptx::mbar_init(pfull(i), 1);
+        ptx::mbar_init(pempty(i), 1);
+      }
+    }
     for (int r = 0; r < kRaw; ++r) {
       ptx::mbar_init(raw_full(r), kRawArrivals);
       ptx::mbar_init(raw_empty(r), kConverters1 / 32);
@@ -1192,13 +1281,18 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           record_error(err_flag, kErrFullWait);
           break;
         }
+        const int sb = kPanel ? static_cast<int>(s % kPanelStages) : st;
+        if (kPanel && !ptx::mbar_wait(pfull(sb), static_cast<uint32_t>((s / kPanelStages) & 1))) {
+          record_error(err_flag, kErrFullWait);
+          break;
+        }
         ptx::tc_fence_after();
         const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
         const uint32_t d_corr = tmem + kCorrCol;
         if constexpr (!kBF16) {
           const uint32_t a_hi = tmem + kAStageCol + 64u * st;
           const uint32_t a_lo = a_hi + 32u;
-          const uint32_t b_hi = op0 + st * kOpBytes;
+          const uint32_t b_hi = op0 + sb * kOpBytes;
           const uint32_t b_lo = b_hi + kBHalfBytes;
 #pragma unroll
           for (int kk = 0; kk < 4; ++kk) {
@@ -1212,7 +1306,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           // A piece p: 16 TMEM columns at +16p; B piece p: 64-byte half
           // (p & 1) of the rows of B buffer (p >> 1).  K = 16 per MMA.
           const uint32_t a0 = tmem + kAStageCol + 64u * st;
-          const uint32_t bb = op0 + st * kOpBytes;
+          const uint32_t bb = op0 + sb * kOpBytes;
 #pragma unroll
           for (int kk = 0; kk < 2; ++kk) {
             auto bd = [&](int p) {
@@ -1230,6 +1324,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           }
         }
         ptx::mma_commit(empty_bar(st));
+        if (kPanel) ptx::mma_commit(pempty(sb));
         if ((s % kFold) == kFold - 1 || s == ksteps - 1) ptx::mma_commit(chunk_full(buf));
       }
       // Signal the epilogue (also after an abort, so nobody waits forever),
@@ -1272,6 +1367,21 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           if (BMode == kGatherNK) gather_b_stage<8>(args, raw_b(r), lt, n0, k0, K);
         }
         ptx::cp_async_arrive_noinc(raw_full(r));
+      }
+      if (kPanel && lt == 0) {
+        // B panel stage: kPanelBufs 128-byte rows per column, the operand
+        // stage's bytes before the swizzle (the TMA load applies it).
+        const int sb = static_cast<int>(s % kPanelStages);
+        if (!ptx::mbar_wait(pempty(sb), static_cast<uint32_t>(((s / kPanelStages) & 1) ^ 1))) {
+          record_error(err_flag, kErrRawWait);
+          break;
+        }
+        const int x = static_cast<int>((kb / kStepKE + s) * kPanelBufs * 64);
+        ptx::mbar_arrive_expect_tx(pfull(sb), static_cast<uint32_t>(kPanelBufs * kBHalfBytes));
+        ptx::tma_load_2d(op0 + sb * kOpBytes, &maps.b, x, static_cast<int>(n0), pfull(sb));
+        if (kPanelBufs == 2)
+          ptx::tma_load_2d(op0 + sb * kOpBytes + kBHalfBytes, &maps.b, x + 64, static_cast<int>(n0),
+                           pfull(sb));
       }
     }
   } else {
@@ -1368,7 +1478,8 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         break;
       }
       // A: kAK1 complex k (this warpgroup's share of the step) of row ci.
-      const uint32_t ra = raw_a(r), rb = raw_b(r);
+      const uint32_t ra = raw_a(r);
+      [[maybe_unused]] const uint32_t rb = raw_b(r);
       // Complex: av[j] = (re, im) of complex k.  Real: av[j] = values of the
       // k pair 2j, 2j + 1 of the lane's row.
       float2 av[kAK1];
@@ -1387,9 +1498,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
 #pragma unroll
         for (int j = 0; j < kAK1; ++j) av[j] = lds64(ra + aoff[j]);
       }
-      // B: this thread's 16-byte pieces (two complex each) of the raw tile.
+      // B: this thread's 16-byte pieces (two complex each) of the raw tile
+      // (none with panels: B arrives split).
       float4 bv[kBV];
-      if constexpr (!kBF16) {
+      if constexpr (kPanel) {
+      } else if constexpr (!kBF16) {
 #pragma unroll
         for (int j = 0; j < kBP1; ++j) {
           if (kReal && BMode == kTmaKN) {
@@ -1427,33 +1540,47 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       // TMA (async proxy) refills it, and generic-proxy reads that are not
       // ordered before that by a proxy fence can observe the refill.
 
+      // A: the 1M rows of this thread's kAK1 complex k, [re, -im] (part 0) or
+      // [im, re] (part 1), real: the pair as is; rows past M arrive as zeros
+      // (TMA out-of-bounds fill, gather zero fill).  Split into registers
+      // before the operand wait: only the stores follow it, which shortens
+      // the round trip from an MMA stage's release to the next stage's
+      // arrival (two A stages fit in TMEM, so that round trip must finish
+      // within one stage of MMAs).
+      uint32_t w[3][kAK1];                  // bf16: piece p of pair j
+      uint32_t hi[2 * kAK1], lo[2 * kAK1];  // TF32: hi / lo of each value
+#pragma unroll
+      for (int j = 0; j < kAK1; ++j) {
+        float2 v = av[j];
+        if (conjA) v.y = -v.y;
+        const float x0 = kReal ? v.x : (part ? v.y : v.x);
+        const float x1 = kReal ? v.y : (part ? v.x : -v.y);
+        if constexpr (kBF16) {
+          split_bf16<kPieces>(x0, x1, w[0][j], w[1][j], w[2][j]);
+        } else {
+          const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
+          hi[2 * j] = s0.hi;
+          lo[2 * j] = s0.lo;
+          hi[2 * j + 1] = s1.hi;
+          lo[2 * j + 1] = s1.lo;
+        }
+      }
+
       if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
         record_error(err_flag, kErrEmptyWait);
         ok = false;
         break;
       }
       ptx::tc_fence_after();
-      const uint32_t ob = op0 + st * kOpBytes;
+      [[maybe_unused]] const uint32_t ob = op0 + st * kOpBytes;
       if constexpr (kBF16) {
-        // A -> TMEM: the 1M row pairs of this thread's kAK1 complex k, split
-        // into kPieces bf16x2 words each; piece p at columns +16p.
-        uint32_t w[3][kAK1];
-#pragma unroll
-        for (int j = 0; j < kAK1; ++j) {
-          float2 v = av[j];
-          if (conjA) v.y = -v.y;
-          if (!row_ok) v = make_float2(0.f, 0.f);
-          // 1M rows [re, -im] (part 0) / [im, re] (part 1); real: the pair as is.
-          const float x0 = kReal ? v.x : (part ? v.y : v.x);
-          const float x1 = kReal ? v.y : (part ? v.x : -v.y);
-          split_bf16<kPieces>(x0, x1, w[0][j], w[1][j], w[2][j]);
-        }
+        // A -> TMEM: kPieces bf16x2 words per pair, piece p at columns +16p.
         const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + kAK1 * wg;
 #pragma unroll
         for (int p = 0; p < kPieces; ++p) ptx::tmem_st_n<kAK1>(a_col + 16u * p, w[p]);
         // B -> shared memory: 4 complex k of column n, re/im interleaved.
 #pragma unroll
-        for (int j = 0; j < kB16P1; ++j) {
+        for (int j = 0; j < (kPanel ? 0 : kB16P1); ++j) {
           float4 v0 = bv[2 * j], v1 = bv[2 * j + 1];
           if (conjB) {
             v0.y = -v0.y;
@@ -1472,28 +1599,13 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
                    qw[0][p], qw[1][p], qw[2][p], qw[3][p]);
         }
       } else {
-        // A -> TMEM: 1M rows, [re, -im] (part 0) or [im, re] (part 1) per k.
-        uint32_t hi[2 * kAK1], lo[2 * kAK1];
-#pragma unroll
-        for (int j = 0; j < kAK1; ++j) {
-          float2 v = av[j];
-          if (conjA) v.y = -v.y;
-          if (!row_ok) v = make_float2(0.f, 0.f);
-          // 1M rows [re, -im] (part 0) / [im, re] (part 1); real: the pair as is.
-          const float x0 = kReal ? v.x : (part ? v.y : v.x);
-          const float x1 = kReal ? v.y : (part ? v.x : -v.y);
-          const Split s0 = split_tf32(x0), s1 = split_tf32(x1);
-          hi[2 * j] = s0.hi;
-          lo[2 * j] = s0.lo;
-          hi[2 * j + 1] = s1.hi;
-          lo[2 * j + 1] = s1.lo;
-        }
+        // A -> TMEM: hi and lo of each value.
         const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + 2 * kAK1 * wg;
         ptx::tmem_st_n<2 * kAK1>(a_col, hi);
         ptx::tmem_st_n<2 * kAK1>(a_col + 32u, lo);
         // B -> shared memory (swizzled K-major hi and lo tiles).
 #pragma unroll
-        for (int j = 0; j < kBP1; ++j) {
+        for (int j = 0; j < (kPanel ? 0 : kBP1); ++j) {
           float4 v = bv[j];
           if (conjB) {
             v.y = -v.y;
@@ -1521,8 +1633,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         ptx::mbar_arrive(raw_empty(r));
       }
 
-      // Fold the previous chunk once the first stage of the next is queued.
-      if ((s % kFold) == 0 && s >= kFold) {
+      // Fold chunk c at stage 4 (c + 1) + 1: the operand wait above already
+      // covered the MMAs of stage 4 c + 3 (the chunk's last), so the chunk
+      // wait does not stall the next conversion.  The chunk's buffer is next
+      // written by chunk c + 2, from stage 4 (c + 2).
+      if ((s % kFold) == 1 && s > kFold) {
         const int64_t c = s / kFold - 1;
         const int buf = static_cast<int>(c & 1);
         if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
@@ -1553,8 +1668,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     }
     ptx::tc_fence_after();
     if (ok) {
-      // The last chunk was never folded in the loop; then add the corrections.
+      // Chunks the loop did not fold: the last, and the one before it when
+      // the last has a single stage; then add the corrections.
       const int64_t c_last = (ksteps - 1) / kFold;
+      if (c_last >= 1 && ksteps < kFold * c_last + 2)
+        fold_from(((c_last - 1) & 1) ? kChunkCol1 : kChunkCol0);
       fold_from((c_last & 1) ? kChunkCol1 : kChunkCol0);
       fold_from(kCorrCol);
       if constexpr (kReal) {
@@ -1634,7 +1752,7 @@ bool unit_blocks16(const std::vector<int64_t>& v, int64_t n) {
 template <int AMode, int BMode, int Prec, bool kReal>
 cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
                          int* err_flag, dim3 tiles) {
-  constexpr int kSmem = smem_bytes_1<kReal>();
+  constexpr int kSmem = smem_bytes_1<kReal, BMode == kPanelNK>();
   static_assert(kSmem <= 227 * 1024, "shared memory budget");
   static bool attr_set = false;
   if (!attr_set) {
@@ -1654,6 +1772,7 @@ cudaError_t launch_b(int bmode, const GemmArgs& args, const TmaMaps& maps, cudaS
   switch (bmode) {
     case kTmaNK: return launch_modes<AMode, kTmaNK, Prec, kReal>(args, maps, stream, err_flag, tiles);
     case kTmaKN: return launch_modes<AMode, kTmaKN, Prec, kReal>(args, maps, stream, err_flag, tiles);
+    case kPanelNK: return launch_modes<AMode, kPanelNK, Prec, kReal>(args, maps, stream, err_flag, tiles);
     default: return launch_modes<AMode, kGatherNK, Prec, kReal>(args, maps, stream, err_flag, tiles);
   }
 }
@@ -1679,6 +1798,49 @@ cudaError_t launch_prec(int method, int amode, int bmode, const GemmArgs& args,
     default:
       return launch_a<kPrecTF32x3, kReal>(amode, bmode, args, maps, stream, err_flag, tiles);
   }
+}
+
+// B panels pay off when enough M tiles share them (each M tile otherwise
+// splits B itself; a panel costs a read of B and a write and read of the
+// panel array, two or three times B's bytes).
+constexpr int64_t kPanelMinTilesM = 4;
+
+int64_t panel_stages(bool real, int64_t K) { return (K + (real ? 32 : 16) - 1) / (real ? 32 : 16); }
+
+// Map over the panel array: rows n, each nstages x bufs x 128 bytes,
+// loaded as 64 x 128 boxes of 16-bit units with the 128-byte swizzle.
+bool make_map_panel(CUtensorMap* map, const void* base, int64_t nstages, int bufs, int64_t N) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  const int64_t units = nstages * bufs * 64;
+  if (units >= (int64_t(1) << 31) || N >= (int64_t(1) << 31) || N <= 0) return false;
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(units), static_cast<cuuint64_t>(N)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(units * 2)};
+  cuuint32_t box[2] = {64, static_cast<cuuint32_t>(kTileN)};
+  cuuint32_t estr[2] = {1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void*>(base), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <bool kReal>
+cudaError_t launch_panels(int method, const GemmArgs& g, void* out, int64_t nstages,
+                          cudaStream_t stream) {
+  const int64_t threads = g.N * nstages;
+  const unsigned blocks = static_cast<unsigned>((threads + 255) / 256);
+  uint4* o = static_cast<uint4*>(out);
+  const int kf = g.uB_k == 1 ? 1 : 0;
+  switch (method) {
+    case T1M_METHOD_TC_BF16X3:
+      split_b_panels<kPrecBF16x3, kReal><<<blocks, 256, 0, stream>>>(g, o, nstages, kf);
+      break;
+    case T1M_METHOD_TC_BF16X6:
+      split_b_panels<kPrecBF16x6, kReal><<<blocks, 256, 0, stream>>>(g, o, nstages, kf);
+      break;
+    default:
+      split_b_panels<kPrecTF32x3, kReal><<<blocks, 256, 0, stream>>>(g, o, nstages, kf);
+  }
+  return cudaGetLastError();
 }
 
 // 2-D map over float32 data: dim0 = inner floats (unit stride), dim1 =
@@ -1958,9 +2120,17 @@ cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_g
   return cudaGetLastError();
 }
 
+size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
+  const bool real = dtype == T1M_FLOAT32;
+  if ((dtype != T1M_COMPLEX64 && !real) || M <= 0 || N <= 0 || K <= 0) return 0;
+  const int64_t rows = real ? 128 : kTileMc;
+  if ((M + rows - 1) / rows < kPanelMinTilesM) return 0;
+  return static_cast<size_t>(N) * static_cast<size_t>(panel_stages(real, K)) * 256u;
+}
+
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
-                      std::string* err, int* used_method) {
+                      std::string* err, int* used_method, void* panel, size_t panel_bytes) {
   *kernels = 0;
   if (used_method) *used_method = method;
   if (!tc_supported(method, dtype, plan)) {
@@ -1968,20 +2138,48 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     return cudaErrorNotSupported;
   }
   if (args.M == 0 || args.N == 0) return cudaSuccess;
-  if (dtype == T1M_FLOAT32) {
-    // Real float32: the one-tile kernel with uniform-view TMA or gathers.
+  const bool real = dtype == T1M_FLOAT32;
+  // B panels: enough M tiles share B and the workspace holds them.  They are
+  // used where they measured faster on GB300: for 3xTF32 (199 vs 192
+  // TFLOP/s at complex64 4096^3; its converters split B into twice the
+  // bytes of bf16 pieces) and for B that would otherwise be gathered.  The
+  // bf16 methods with a TMA-loadable B keep the in-kernel split (204 vs 197
+  // TFLOP/s with panels: the panel pass is not repaid there).
+  const size_t need = tc_panel_bytes(dtype, args.M, args.N, args.K);
+  const bool panels_ok = panel && need > 0 && panel_bytes >= need;
+  auto want_panels = [&](bool b_gathered) {
+    return panels_ok && (b_gathered || method == T1M_METHOD_TC_3XTF32);
+  };
+  const int64_t nstages = panel_stages(real, args.K);
+  // Split B into the panels and point the kernel's B map at them.
+  auto use_panels = [&](const GemmArgs& g, TmaMaps* maps, int* bm) -> cudaError_t {
+    const int bufs = method == T1M_METHOD_TC_BF16X3 ? 1 : 2;
+    if (!make_map_panel(&maps->b, panel, nstages, bufs, args.N)) return cudaSuccess;
+    const cudaError_t e = real ? launch_panels<true>(method, g, panel, nstages, stream)
+                               : launch_panels<false>(method, g, panel, nstages, stream);
+    if (e == cudaSuccess) {
+      *bm = kPanelNK;
+      ++*kernels;
+    }
+    return e;
+  };
+  if (real) {
+    // Real float32: the one-tile kernel with uniform-view TMA, gathers or panels.
     int am = kGatherMK, bm = kGatherNK;
     TmaMaps maps;
     GemmArgs gr;
     if (!tc_prepare_real(args, plan, splits, &am, &bm, &maps, &gr))
       return cudaErrorInvalidConfiguration;
     if (method == kMethodTcAuto)
-      method = (am != kGatherMK && bm != kGatherNK) ? T1M_METHOD_TC_BF16X6 : T1M_METHOD_TC_3XTF32;
+      method = (am != kGatherMK && (bm != kGatherNK || panels_ok)) ? T1M_METHOD_TC_BF16X6
+                                                                    : T1M_METHOD_TC_3XTF32;
     if (used_method) *used_method = method;
+    if (want_panels(bm == kGatherNK))
+      if (const cudaError_t e = use_panels(gr, &maps, &bm)) return e;
     const dim3 grid(static_cast<unsigned>(((args.M + 127) / 128) * ((args.N + kTileN - 1) / kTileN)),
                     static_cast<unsigned>(splits));
     const cudaError_t e = launch_prec<true>(method, am, bm, gr, maps, stream, err_flag, grid);
-    if (e == cudaSuccess) *kernels = 1;
+    if (e == cudaSuccess) ++*kernels;
     return e;
   }
   TcProblem p;
@@ -1991,37 +2189,41 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   p.dep = -1;
-  cudaError_t e;
+  const bool a_block = (p.block_maps & 1) || p.amode == kAMK16;
+  const bool b_block = (p.block_maps & 2) != 0;
   if (method == kMethodTcAuto) {
     // BF16x6 measured faster than 3xTF32 (203 vs 193-198 TFLOP/s at complex64
     // 4096^3) and more accurate in the one-tile kernel with TMA operands;
     // block-TMA layouts stay on the persistent 3xTF32 kernel.
-    const bool tma_both = p.block_maps == 0 && p.amode != kAMK16 && p.amode != kAGather &&
-                          p.bmode != kBGather;
-    method = tma_both ? T1M_METHOD_TC_BF16X6 : T1M_METHOD_TC_3XTF32;
+    const bool tma_a = !a_block && p.amode != kAGather;
+    const bool tma_b = panels_ok || (!b_block && p.bmode != kBGather);
+    method = (tma_a && tma_b) ? T1M_METHOD_TC_BF16X6 : T1M_METHOD_TC_3XTF32;
     if (used_method) *used_method = method;
   }
   const bool bf16 = method != T1M_METHOD_TC_3XTF32;
-  if (bf16 || (p.block_maps == 0 && p.amode != kAMK16)) {
-    // Uniform or gathered operands: the one-tile-per-CTA form.  The bf16
-    // forms exist only here: an operand that needs a per-block map is
+  const bool b_gathered = b_block || p.bmode == kBGather;
+  const bool panels = want_panels(b_gathered);
+  cudaError_t e;
+  if (bf16 || (!a_block && (!b_block || panels))) {
+    // Uniform, gathered or panel operands: the one-tile-per-CTA form.  The
+    // bf16 forms exist only here: an operand that needs a per-block map is
     // gathered instead.
     TmaMaps maps;
     maps.a = p.map_a;
     maps.b = p.map_b;
     const dim3 grid(static_cast<unsigned>(int64_t(p.tiles_m) * p.tiles_n),
                     static_cast<unsigned>(splits));
-    const bool a_uniform = !(p.block_maps & 1);
-    const bool b_uniform = !(p.block_maps & 2);
-    const int am = (a_uniform && p.amode == kAMK) ? kTmaMK
-                   : (a_uniform && p.amode == kAKM) ? kTmaKM : kGatherMK;
-    const int bm = (b_uniform && p.bmode == kBNK) ? kTmaNK
-                   : (b_uniform && p.bmode == kBKN) ? kTmaKN : kGatherNK;
+    const int am = (!a_block && p.amode == kAMK) ? kTmaMK
+                   : (!a_block && p.amode == kAKM) ? kTmaKM : kGatherMK;
+    int bm = (!b_block && p.bmode == kBNK) ? kTmaNK
+             : (!b_block && p.bmode == kBKN) ? kTmaKN : kGatherNK;
+    if (panels)
+      if ((e = use_panels(p.g, &maps, &bm)) != cudaSuccess) return e;
     e = launch_prec<false>(method, am, bm, p.g, maps, stream, err_flag, grid);
   } else {
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
   }
-  if (e == cudaSuccess) *kernels = 1;
+  if (e == cudaSuccess) ++*kernels;
   return e;
 }
 
