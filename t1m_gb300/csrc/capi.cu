@@ -56,9 +56,11 @@ struct t1m_context {
   // Split-K workspace (grow only) and the forced split count (0 = automatic).
   void* work = nullptr;
   size_t work_bytes = 0;
-  // B-panel workspace of the tensor-core kernels (grow only).
+  // B-panel and operand-pack workspaces of the tensor-core kernels (grow only).
   void* panel = nullptr;
   size_t panel_bytes = 0;
+  void* pack = nullptr;
+  size_t pack_bytes = 0;
   int split_k = 0;
   int num_sms = 152;
   // Host-operand pipeline: copy-in and copy-out streams beside the compute
@@ -249,22 +251,22 @@ int ensure_work(t1m_context* ctx, size_t bytes) {
   return T1M_OK;
 }
 
-// B-panel workspace: the panels are an optimisation, so a failed allocation
-// leaves the product on the converter path instead of failing it.
-bool ensure_panel(t1m_context* ctx, size_t bytes) {
-  if (ctx->panel_bytes >= bytes) return true;
-  if (ctx->panel) {
+// B-panel and operand-pack workspaces: both are optimisations, so a failed
+// allocation leaves the product on the in-kernel path instead of failing it.
+bool ensure_opt_work(t1m_context* ctx, void** buf, size_t* have, size_t bytes) {
+  if (*have >= bytes) return true;
+  if (*buf) {
     cudaStreamSynchronize(ctx->stream);
-    cudaFree(ctx->panel);
+    cudaFree(*buf);
   }
-  ctx->panel = nullptr;
-  ctx->panel_bytes = 0;
-  if (cudaMalloc(&ctx->panel, bytes) != cudaSuccess) {
+  *buf = nullptr;
+  *have = 0;
+  if (cudaMalloc(buf, bytes) != cudaSuccess) {
     cudaGetLastError();
-    ctx->panel = nullptr;
+    *buf = nullptr;
     return false;
   }
-  ctx->panel_bytes = bytes;
+  *have = bytes;
   return true;
 }
 
@@ -318,9 +320,12 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       std::string err;
       int ran = method;
       const size_t pb = tc_panel_bytes(dtype, gm.M, gm.N, gm.K);
-      const bool pan = pb > 0 && ensure_panel(ctx, pb);
+      const bool pan = pb > 0 && ensure_opt_work(ctx, &ctx->panel, &ctx->panel_bytes, pb);
+      const size_t kb = tc_pack_bytes(dtype, hp);
+      const bool pk = kb > 0 && ensure_opt_work(ctx, &ctx->pack, &ctx->pack_bytes, kb);
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
-                    pan ? ctx->panel : nullptr, pan ? ctx->panel_bytes : 0);
+                    pan ? ctx->panel : nullptr, pan ? ctx->panel_bytes : 0,
+                    pk ? ctx->pack : nullptr, pk ? ctx->pack_bytes : 0);
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -591,6 +596,7 @@ int t1m_destroy(t1m_context* ctx) {
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->work) cudaFree(ctx->work);
   if (ctx->panel) cudaFree(ctx->panel);
+  if (ctx->pack) cudaFree(ctx->pack);
   for (int i = 0; i < t1m_context::kPipeEvents; ++i)
     if (ctx->pev[i]) cudaEventDestroy(ctx->pev[i]);
   if (ctx->copy_in) {

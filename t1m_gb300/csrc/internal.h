@@ -172,12 +172,24 @@ cudaError_t launch_splitk_reduce_group(int dtype, const SplitReduce* dev, int n,
 // tc.cu: one contraction on the tensor cores (complex64 / float32, split
 // methods).  `panel` (panel_bytes) is workspace for B split once into
 // panels, at least tc_panel_bytes(dtype, M, N, K) bytes, or null.
+// `pack` (pack_bytes) is workspace for operands repacked densely
+// (tc_pack_bytes), or null.
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel = nullptr,
-                      size_t panel_bytes = 0);
+                      size_t panel_bytes = 0, void* pack = nullptr, size_t pack_bytes = 0);
 // Panel workspace a product would use (0: panels not used at this size).
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K);
+// Pack workspace a product may use (0: neither operand would be packed).
+size_t tc_pack_bytes(int dtype, const HostPlan& plan);
+
+// pack.cu: dst[r * pitch + k] = src[ro(r) + ko(k)] (complex64 or float32),
+// reads coalesced along the source's unit-stride direction: a K mode of
+// k-step S (S > 0), a row mode (S == 0), or none (S < 0).
+int64_t pack_pitch(int dtype, int64_t K);
+cudaError_t launch_pack(int dtype, const void* src, const int64_t* ro, int64_t ur,
+                        const int64_t* ko, int64_t uk, int64_t R, int64_t K, int64_t S,
+                        void* dst, int64_t pitch, cudaStream_t stream);
 bool tc_supported(int method, int dtype, const HostPlan& plan);
 void tc_tile(int dtype, int* bm, int* bn, int* bk);
 

@@ -2120,6 +2120,44 @@ cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_g
   return cudaGetLastError();
 }
 
+// Operands gathered element by element are packed first (pack.cu) when they
+// hold at least this many bytes; below it the extra pass is not repaid.
+constexpr size_t kPackMinBytes = size_t(4) << 20;
+
+// k-step, in the plan's K order, of an operand's unit-stride K mode (> 1); 0
+// when its unit-stride mode is a row mode; -1 when it has none, or when that
+// mode is the first K mode (its k runs are contiguous already).
+int64_t pack_step(const std::vector<Mode>& kmodes, bool second, const std::vector<Mode>& rmodes) {
+  int64_t step = 1;
+  for (const Mode& m : kmodes) {
+    if ((second ? m.s1 : m.s0) == 1 && m.extent > 1) return step > 1 ? step : -1;
+    step *= m.extent;
+  }
+  for (const Mode& m : rmodes)
+    if (m.s0 == 1 && m.extent > 1) return 0;
+  return -1;
+}
+
+// An operand without a uniform view that has a unit-stride direction may be
+// gathered element by element.
+bool gather_prone(int64_t u_row, int64_t u_k) {
+  return !(u_row == 1 && u_k >= 0) && !(u_k == 1 && u_row >= 0);
+}
+
+size_t tc_pack_bytes(int dtype, const HostPlan& plan) {
+  if (dtype != T1M_COMPLEX64 && dtype != T1M_FLOAT32) return 0;
+  const size_t es = dtype == T1M_FLOAT32 ? 4 : 8;
+  const size_t pitch = static_cast<size_t>(pack_pitch(dtype, plan.K));
+  size_t b = 0;
+  if (gather_prone(plan.uA_m, plan.uA_k) &&
+      static_cast<size_t>(plan.M) * static_cast<size_t>(plan.K) * es >= kPackMinBytes)
+    b += static_cast<size_t>(plan.M) * pitch * es;
+  if (gather_prone(plan.uB_n, plan.uB_k) &&
+      static_cast<size_t>(plan.N) * static_cast<size_t>(plan.K) * es >= kPackMinBytes)
+    b += static_cast<size_t>(plan.N) * pitch * es;
+  return b;
+}
+
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
   const bool real = dtype == T1M_FLOAT32;
   if ((dtype != T1M_COMPLEX64 && !real) || M <= 0 || N <= 0 || K <= 0) return 0;
@@ -2130,7 +2168,8 @@ size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
 
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
-                      std::string* err, int* used_method, void* panel, size_t panel_bytes) {
+                      std::string* err, int* used_method, void* panel, size_t panel_bytes,
+                      void* pack, size_t pack_bytes) {
   *kernels = 0;
   if (used_method) *used_method = method;
   if (!tc_supported(method, dtype, plan)) {
@@ -2163,6 +2202,54 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     }
     return e;
   };
+  // Dense repacks of operands the kernels would gather element by element:
+  // *ga / *hp become the problem with the packed operands (uniform, unit K
+  // stride, rows `pitch` apart), loaded by TMA.  A is packed when large; B
+  // when large and the panels (which gather B in their own pass) are not
+  // used.
+  const size_t es = real ? 4 : 8;
+  const int64_t pitch = pack_pitch(dtype, args.K);
+  const bool a_big = static_cast<size_t>(args.M) * static_cast<size_t>(args.K) * es >= kPackMinBytes;
+  const bool b_big = static_cast<size_t>(args.N) * static_cast<size_t>(args.K) * es >= kPackMinBytes;
+  auto pack_operands = [&](bool pa, bool pb, GemmArgs* ga, HostPlan* hp) -> cudaError_t {
+    const size_t bytes = (static_cast<size_t>(pa ? args.M : 0) + (pb ? args.N : 0)) *
+                         static_cast<size_t>(pitch) * es;
+    if (!pack || bytes == 0 || pack_bytes < bytes) return cudaSuccess;
+    *hp = plan;
+    char* dst = static_cast<char*>(pack);
+    if (pa) {
+      const cudaError_t e = launch_pack(dtype, args.A, args.rsA, args.uA_m, args.csA, args.uA_k,
+                                        args.M, args.K, pack_step(plan.modes_k, false, plan.modes_m),
+                                        dst, pitch, stream);
+      if (e != cudaSuccess) return e;
+      ga->A = dst;
+      ga->rsA = ga->csA = nullptr;
+      ga->uA_m = hp->uA_m = pitch;
+      ga->uA_k = hp->uA_k = 1;
+      for (int64_t i = 0; i < args.M; ++i) hp->rsA[i] = i * pitch;
+      for (int64_t i = 0; i < args.K; ++i) hp->csA[i] = i;
+      hp->spanA = args.M * pitch;
+      dst += static_cast<size_t>(args.M) * static_cast<size_t>(pitch) * es;
+      ++*kernels;
+    }
+    if (pb) {
+      const cudaError_t e = launch_pack(dtype, args.B, args.csB, args.uB_n, args.rsB, args.uB_k,
+                                        args.N, args.K, pack_step(plan.modes_k, true, plan.modes_n),
+                                        dst, pitch, stream);
+      if (e != cudaSuccess) return e;
+      ga->B = dst;
+      ga->rsB = ga->csB = nullptr;
+      ga->uB_n = hp->uB_n = pitch;
+      ga->uB_k = hp->uB_k = 1;
+      for (int64_t i = 0; i < args.N; ++i) hp->csB[i] = i * pitch;
+      for (int64_t i = 0; i < args.K; ++i) hp->rsB[i] = i;
+      hp->spanB = args.N * pitch;
+      ++*kernels;
+    }
+    return cudaSuccess;
+  };
+  GemmArgs packed_args = args;
+  HostPlan packed_plan;
   if (real) {
     // Real float32: the one-tile kernel with uniform-view TMA, gathers or panels.
     int am = kGatherMK, bm = kGatherNK;
@@ -2170,6 +2257,15 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     GemmArgs gr;
     if (!tc_prepare_real(args, plan, splits, &am, &bm, &maps, &gr))
       return cudaErrorInvalidConfiguration;
+    const bool pa = am == kGatherMK && a_big;
+    const bool pb = bm == kGatherNK && b_big && !panels_ok;
+    if (pa || pb) {
+      const int before = *kernels;
+      if (const cudaError_t e = pack_operands(pa, pb, &packed_args, &packed_plan)) return e;
+      if (*kernels != before &&
+          !tc_prepare_real(packed_args, packed_plan, splits, &am, &bm, &maps, &gr))
+        return cudaErrorInvalidConfiguration;
+    }
     if (method == kMethodTcAuto)
       method = (am != kGatherMK && (bm != kGatherNK || panels_ok)) ? T1M_METHOD_TC_BF16X6
                                                                     : T1M_METHOD_TC_3XTF32;
@@ -2184,6 +2280,16 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   }
   TcProblem p;
   if (!tc_prepare(args, plan, splits, &p)) return cudaErrorInvalidConfiguration;
+  {
+    const bool pa = p.amode == kAGather && a_big;
+    const bool pb = p.bmode == kBGather && b_big && !panels_ok;
+    if (pa || pb) {
+      const int before = *kernels;
+      if (const cudaError_t e = pack_operands(pa, pb, &packed_args, &packed_plan)) return e;
+      if (*kernels != before && !tc_prepare(packed_args, packed_plan, splits, &p))
+        return cudaErrorInvalidConfiguration;
+    }
+  }
   p.tile_begin = 0;
   int dev = 0, sms = 152;
   cudaGetDevice(&dev);

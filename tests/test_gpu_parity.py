@@ -202,7 +202,10 @@ def test_config2_full_size_tensor_core(ctx, torch_cuda, cfg, layout):
     assert mx < 1e-6 and fro < 1e-6, (mx, fro, rep.split_k)
     assert rep.method == 2
     if cfg == 1:
-        assert rep.split_k > 1 and rep.kernels == 2
+        # Split-K with its FP64 reduction, after dense packs of the operands
+        # that would be gathered element by element: A (col-major), A and B
+        # (row-major, where B's 24-element runs of a straddle 16-element blocks).
+        assert rep.split_k > 1 and rep.kernels == (3 if layout == "col" else 4), rep.kernels
     ctx.set_method("auto")
 
 
