@@ -3,7 +3,10 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
+#include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -47,6 +50,12 @@ struct HostPlan {
   int64_t uA_m = -1, uA_k = -1, uB_k = -1, uB_n = -1, uC_m = -1, uC_n = -1;
   // Number of elements each tensor spans in memory (1 + sum (e-1)*s).
   int64_t spanA = 0, spanB = 0, spanC = 0;
+  // Derived once per plan (the context caches plans across calls): results
+  // of the tensor-core path's layout checks over the scatter vectors, keyed
+  // by check and length, and the plans with densely packed operands (index
+  // 1: A packed, 2: B packed, 3: both).
+  mutable std::map<std::pair<int, int64_t>, int64_t> memo;
+  mutable std::shared_ptr<HostPlan> packed[4];
 };
 
 // Element offsets of batch index `bi` (mixed radix over modes_b, first mode

@@ -2022,6 +2022,38 @@ bool tc_supported(int method, int dtype, const HostPlan& plan) {
          (dtype == T1M_COMPLEX64 || dtype == T1M_FLOAT32);
 }
 
+// The layout checks over the scatter vectors depend only on the plan and the
+// length checked (slabs of a pipelined product check shorter prefixes), so
+// they are memoised in the plan.
+enum : int {
+  kChkUnitRsA = 1, kChkUnitCsA, kChkUnitRsB, kChkUnitCsB,
+  kChkStrideRsA, kChkStrideCsA, kChkStrideCsB, kChkStrideRsB
+};
+constexpr int64_t kNoStride = INT64_MIN;
+
+bool unit16(const HostPlan& plan, int which, const std::vector<int64_t>& v, int64_t n) {
+  const auto key = std::make_pair(which, n);
+  const auto it = plan.memo.find(key);
+  if (it != plan.memo.end()) return it->second != 0;
+  const bool r = unit_blocks16(v, n);
+  plan.memo[key] = r ? 1 : 0;
+  return r;
+}
+
+bool stride16(const HostPlan& plan, int which, const std::vector<int64_t>& rows,
+              const std::vector<int64_t>& runs, int64_t n, int64_t* stride) {
+  const auto key = std::make_pair(which, n);
+  const auto it = plan.memo.find(key);
+  if (it != plan.memo.end()) {
+    if (it->second == kNoStride) return false;
+    *stride = it->second;
+    return true;
+  }
+  const bool r = common_block_stride16(rows, runs, n, stride);
+  plan.memo[key] = r ? *stride : kNoStride;
+  return r;
+}
+
 bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p) {
   std::memset(static_cast<void*>(p), 0, sizeof(*p));
   p->g = g;
@@ -2039,21 +2071,21 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
   else if (plan.uA_k == 1 && plan.uA_m >= 0 &&
            make_map(&p->map_a, g.A, g.K, g.M, plan.uA_m, 2 * kStepK, kTileMc, true))
     p->amode = kAKM;
-  else if (plan.uA_k >= 0 && unit_blocks16(plan.rsA, g.M) &&
+  else if (plan.uA_k >= 0 && unit16(plan, kChkUnitRsA, plan.rsA, g.M) &&
            make_map(&p->map_a, g.A, plan.spanA, g.K, plan.uA_k, 32, kStepK, false)) {
     p->amode = kAMK16;
     p->block_maps |= 1;
-  } else if (plan.uA_m >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.csA, g.K) &&
+  } else if (plan.uA_m >= 0 && g.K % kStepK == 0 && unit16(plan, kChkUnitCsA, plan.csA, g.K) &&
              make_map(&p->map_a, g.A, plan.spanA, g.M, plan.uA_m, 2 * kStepK, kTileMc, true)) {
     p->amode = kAKM;
     p->block_maps |= 1;
-  } else if (int64_t sm = 0; g.K % kStepK == 0 && unit_blocks16(plan.csA, g.K) &&
-                             common_block_stride16(plan.rsA, plan.csA, g.M, &sm) &&
+  } else if (int64_t sm = 0; g.K % kStepK == 0 && unit16(plan, kChkUnitCsA, plan.csA, g.K) &&
+                             stride16(plan, kChkStrideRsA, plan.rsA, plan.csA, g.M, &sm) &&
                              make_map(&p->map_a, g.A, plan.spanA, 16, sm, 2 * kStepK, 16, true)) {
     p->amode = kAKM16;
     p->block_maps |= 1;
-  } else if (int64_t sk = 0; g.M % 16 == 0 && unit_blocks16(plan.rsA, g.M) &&
-                             common_block_stride16(plan.csA, plan.rsA, g.K, &sk) &&
+  } else if (int64_t sk = 0; g.M % 16 == 0 && unit16(plan, kChkUnitRsA, plan.rsA, g.M) &&
+                             stride16(plan, kChkStrideCsA, plan.csA, plan.rsA, g.K, &sk) &&
                              make_map(&p->map_a, g.A, plan.spanA, 16, sk, 32, 16, false)) {
     p->amode = kAMK16K;
     p->block_maps |= 1;
@@ -2066,17 +2098,17 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
   else if (plan.uB_n == 1 && plan.uB_k >= 0 &&
            make_map(&p->map_b, g.B, g.N, g.K, plan.uB_k, 2 * kTileN, kStepK, false))
     p->bmode = kBKN;
-  else if (plan.uB_n >= 0 && g.K % kStepK == 0 && unit_blocks16(plan.rsB, g.K) &&
+  else if (plan.uB_n >= 0 && g.K % kStepK == 0 && unit16(plan, kChkUnitRsB, plan.rsB, g.K) &&
            make_map(&p->map_b, g.B, plan.spanB, g.N, plan.uB_n, 2 * kStepK, kTileN, true)) {
     p->bmode = kBNK;
     p->block_maps |= 2;
-  } else if (int64_t sn = 0; g.K % kStepK == 0 && unit_blocks16(plan.rsB, g.K) &&
-                             common_block_stride16(plan.csB, plan.rsB, g.N, &sn) &&
+  } else if (int64_t sn = 0; g.K % kStepK == 0 && unit16(plan, kChkUnitRsB, plan.rsB, g.K) &&
+                             stride16(plan, kChkStrideCsB, plan.csB, plan.rsB, g.N, &sn) &&
                              make_map(&p->map_b, g.B, plan.spanB, 16, sn, 2 * kStepK, 16, true)) {
     p->bmode = kBNK16;
     p->block_maps |= 2;
-  } else if (int64_t sk = 0; g.N % 16 == 0 && unit_blocks16(plan.csB, g.N) &&
-                             common_block_stride16(plan.rsB, plan.csB, g.K, &sk) &&
+  } else if (int64_t sk = 0; g.N % 16 == 0 && unit16(plan, kChkUnitCsB, plan.csB, g.N) &&
+                             stride16(plan, kChkStrideRsB, plan.rsB, plan.csB, g.K, &sk) &&
                              make_map(&p->map_b, g.B, plan.spanB, 16, sk, 32, 16, false)) {
     p->bmode = kBKN16;
     p->block_maps |= 2;
@@ -2211,11 +2243,34 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   const int64_t pitch = pack_pitch(dtype, args.K);
   const bool a_big = static_cast<size_t>(args.M) * static_cast<size_t>(args.K) * es >= kPackMinBytes;
   const bool b_big = static_cast<size_t>(args.N) * static_cast<size_t>(args.K) * es >= kPackMinBytes;
-  auto pack_operands = [&](bool pa, bool pb, GemmArgs* ga, HostPlan* hp) -> cudaError_t {
+  auto pack_operands = [&](bool pa, bool pb, GemmArgs* ga, const HostPlan** hp) -> cudaError_t {
     const size_t bytes = (static_cast<size_t>(pa ? args.M : 0) + (pb ? args.N : 0)) *
                          static_cast<size_t>(pitch) * es;
     if (!pack || bytes == 0 || pack_bytes < bytes) return cudaSuccess;
-    *hp = plan;
+    // The plan of the packed problem: uniform, unit K stride, rows `pitch`
+    // apart for each packed operand (built once per plan and kept in it).
+    std::shared_ptr<HostPlan>& slot = plan.packed[(pa ? 1 : 0) | (pb ? 2 : 0)];
+    if (!slot) {
+      auto q = std::make_shared<HostPlan>(plan);
+      q->memo.clear();
+      for (auto& x : q->packed) x.reset();
+      if (pa) {
+        q->uA_m = pitch;
+        q->uA_k = 1;
+        for (int64_t i = 0; i < plan.M; ++i) q->rsA[i] = i * pitch;
+        for (int64_t i = 0; i < plan.K; ++i) q->csA[i] = i;
+        q->spanA = plan.M * pitch;
+      }
+      if (pb) {
+        q->uB_n = pitch;
+        q->uB_k = 1;
+        for (int64_t i = 0; i < plan.N; ++i) q->csB[i] = i * pitch;
+        for (int64_t i = 0; i < plan.K; ++i) q->rsB[i] = i;
+        q->spanB = plan.N * pitch;
+      }
+      slot = std::move(q);
+    }
+    *hp = slot.get();
     char* dst = static_cast<char*>(pack);
     if (pa) {
       const cudaError_t e = launch_pack(dtype, args.A, args.rsA, args.uA_m, args.csA, args.uA_k,
@@ -2224,11 +2279,8 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
       if (e != cudaSuccess) return e;
       ga->A = dst;
       ga->rsA = ga->csA = nullptr;
-      ga->uA_m = hp->uA_m = pitch;
-      ga->uA_k = hp->uA_k = 1;
-      for (int64_t i = 0; i < args.M; ++i) hp->rsA[i] = i * pitch;
-      for (int64_t i = 0; i < args.K; ++i) hp->csA[i] = i;
-      hp->spanA = args.M * pitch;
+      ga->uA_m = pitch;
+      ga->uA_k = 1;
       dst += static_cast<size_t>(args.M) * static_cast<size_t>(pitch) * es;
       ++*kernels;
     }
@@ -2239,17 +2291,14 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
       if (e != cudaSuccess) return e;
       ga->B = dst;
       ga->rsB = ga->csB = nullptr;
-      ga->uB_n = hp->uB_n = pitch;
-      ga->uB_k = hp->uB_k = 1;
-      for (int64_t i = 0; i < args.N; ++i) hp->csB[i] = i * pitch;
-      for (int64_t i = 0; i < args.K; ++i) hp->rsB[i] = i;
-      hp->spanB = args.N * pitch;
+      ga->uB_n = pitch;
+      ga->uB_k = 1;
       ++*kernels;
     }
     return cudaSuccess;
   };
   GemmArgs packed_args = args;
-  HostPlan packed_plan;
+  const HostPlan* packed_plan = &plan;
   if (real) {
     // Real float32: the one-tile kernel with uniform-view TMA, gathers or panels.
     int am = kGatherMK, bm = kGatherNK;
@@ -2263,7 +2312,7 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
       const int before = *kernels;
       if (const cudaError_t e = pack_operands(pa, pb, &packed_args, &packed_plan)) return e;
       if (*kernels != before &&
-          !tc_prepare_real(packed_args, packed_plan, splits, &am, &bm, &maps, &gr))
+          !tc_prepare_real(packed_args, *packed_plan, splits, &am, &bm, &maps, &gr))
         return cudaErrorInvalidConfiguration;
     }
     if (method == kMethodTcAuto)
@@ -2286,7 +2335,7 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     if (pa || pb) {
       const int before = *kernels;
       if (const cudaError_t e = pack_operands(pa, pb, &packed_args, &packed_plan)) return e;
-      if (*kernels != before && !tc_prepare(packed_args, packed_plan, splits, &p))
+      if (*kernels != before && !tc_prepare(packed_args, *packed_plan, splits, &p))
         return cudaErrorInvalidConfiguration;
     }
   }
