@@ -40,6 +40,10 @@ pack_tiled(const T* __restrict__ src, const int64_t* __restrict__ ro, int64_t ur
            const int64_t* __restrict__ ko, int64_t uk, int64_t R, int64_t K, int64_t S,
            T* __restrict__ dst, int64_t pitch, int64_t tiles_a, int64_t tiles_b) {
   __shared__ T tile[32][33];
+  // Source offsets of the tile's 32 + 32 index values, loaded once per tile:
+  // offsets are linear in the mode indices and S spans whole modes, so
+  // ko(k_lo + S k_hi) = ko(k_lo) + ko(S k_hi) (and src(r, k) = ro(r) + ko(k)).
+  __shared__ int64_t off_a[32], off_b[32];
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 8 warps
   // Tile coordinates: S > 0: (row r, k_hi tile ta, k_lo tile tb);
   // S == 0: (row tile ta, k tile tb).
@@ -49,26 +53,40 @@ pack_tiled(const T* __restrict__ src, const int64_t* __restrict__ ro, int64_t ur
   const int64_t ta = t % tiles_a;
   const int64_t r0 = t / tiles_a;
   if (S > 0) {
-    const int64_t nhi = (K + S - 1) / S;
+    const int64_t nhi = K / S;  // S is a product of leading K extents
+    if (threadIdx.x < 32) {
+      const int64_t khi = ta * 32 + threadIdx.x;
+      off_a[threadIdx.x] = khi < nhi ? poffs(ko, uk, S * khi) : 0;
+    } else if (threadIdx.x < 64) {
+      const int64_t klo = tb * 32 + threadIdx.x - 32;
+      off_b[threadIdx.x - 32] = klo < S ? poffs(ko, uk, klo) : 0;
+    }
+    __syncthreads();
+    const int64_t rbase = poffs(ro, ur, r0);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int64_t klo = tb * 32 + ty + 8 * i, khi = ta * 32 + tx;
-      const int64_t k = klo + S * khi;
-      if (klo < S && khi < nhi && k < K)
-        tile[ty + 8 * i][tx] = src[poffs(ro, ur, r0) + poffs(ko, uk, k)];
+      if (klo < S && khi < nhi) tile[ty + 8 * i][tx] = src[rbase + off_b[ty + 8 * i] + off_a[tx]];
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int64_t klo = tb * 32 + tx, khi = ta * 32 + ty + 8 * i;
-      const int64_t k = klo + S * khi;
-      if (klo < S && khi < nhi && k < K) dst[r0 * pitch + k] = tile[tx][ty + 8 * i];
+      if (klo < S && khi < nhi) dst[r0 * pitch + klo + S * khi] = tile[tx][ty + 8 * i];
     }
   } else {
+    if (threadIdx.x < 32) {
+      const int64_t r = ta * 32 + threadIdx.x;
+      off_a[threadIdx.x] = r < R ? poffs(ro, ur, r) : 0;
+    } else if (threadIdx.x < 64) {
+      const int64_t k = tb * 32 + threadIdx.x - 32;
+      off_b[threadIdx.x - 32] = k < K ? poffs(ko, uk, k) : 0;
+    }
+    __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       const int64_t r = ta * 32 + tx, k = tb * 32 + ty + 8 * i;
-      if (r < R && k < K) tile[ty + 8 * i][tx] = src[poffs(ro, ur, r) + poffs(ko, uk, k)];
+      if (r < R && k < K) tile[ty + 8 * i][tx] = src[off_a[tx] + off_b[ty + 8 * i]];
     }
     __syncthreads();
 #pragma unroll

@@ -1067,22 +1067,52 @@ split_b_panels(const GemmArgs g, uint4* __restrict__ out, int64_t nstages, int k
   const int64_t s = k_fastest ? idx % nstages : idx / g.N;
   const int64_t cn = offs(g.csB, g.uB_n, n);
   float v[32];
+  // A full stage of a unit-K-stride column, 16-byte aligned, is read as eight
+  // 16-byte loads; otherwise element by element through the K offsets.
   if constexpr (kReal) {
     const float* __restrict__ B = static_cast<const float*>(g.B);
+    const float* col = B + cn + 32 * s;
+    if (g.uB_k == 1 && 32 * s + 32 <= g.K && (reinterpret_cast<uintptr_t>(col) & 15u) == 0) {
 #pragma unroll
-    for (int j = 0; j < 32; ++j) {
-      const int64_t k = 32 * s + j;
-      v[j] = k < g.K ? B[cn + offs(g.rsB, g.uB_k, k)] : 0.f;
+      for (int j = 0; j < 8; ++j) {
+        const float4 q = reinterpret_cast<const float4*>(col)[j];
+        v[4 * j] = q.x;
+        v[4 * j + 1] = q.y;
+        v[4 * j + 2] = q.z;
+        v[4 * j + 3] = q.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int64_t k = 32 * s + j;
+        v[j] = k < g.K ? B[cn + offs(g.rsB, g.uB_k, k)] : 0.f;
+      }
     }
   } else {
     const float2* __restrict__ B = static_cast<const float2*>(g.B);
     const bool conj = g.flags & kFlagConjB;
+    const float2* col = B + cn + 16 * s;
+    if (g.uB_k == 1 && 16 * s + 16 <= g.K && (reinterpret_cast<uintptr_t>(col) & 15u) == 0) {
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      const int64_t k = 16 * s + j;
-      const float2 x = k < g.K ? B[cn + offs(g.rsB, g.uB_k, k)] : make_float2(0.f, 0.f);
-      v[2 * j] = x.x;
-      v[2 * j + 1] = conj ? -x.y : x.y;
+      for (int j = 0; j < 8; ++j) {
+        const float4 q = reinterpret_cast<const float4*>(col)[j];
+        v[4 * j] = q.x;
+        v[4 * j + 1] = q.y;
+        v[4 * j + 2] = q.z;
+        v[4 * j + 3] = q.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int64_t k = 16 * s + j;
+        const float2 x = k < g.K ? B[cn + offs(g.rsB, g.uB_k, k)] : make_float2(0.f, 0.f);
+        v[2 * j] = x.x;
+        v[2 * j + 1] = x.y;
+      }
+    }
+    if (conj) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) v[2 * j + 1] = -v[2 * j + 1];
     }
   }
   uint4* __restrict__ row = out + (n * nstages + s) * (8 * kBufs);
