@@ -56,17 +56,22 @@ struct t1m_context {
   // Split-K workspace (grow only) and the forced split count (0 = automatic).
   void* work = nullptr;
   size_t work_bytes = 0;
-  // B-panel and operand-pack workspaces of the tensor-core kernels (grow only).
-  void* panel = nullptr;
-  size_t panel_bytes = 0;
-  void* pack = nullptr;
-  size_t pack_bytes = 0;
+  // B-panel and operand-pack workspaces of the tensor-core kernels (grow
+  // only), one set per compute stream of the slab pipeline.
+  void* panel[2] = {nullptr, nullptr};
+  size_t panel_bytes[2] = {0, 0};
+  void* pack[2] = {nullptr, nullptr};
+  size_t pack_bytes[2] = {0, 0};
   int split_k = 0;
   int num_sms = 152;
   // Host-operand pipeline: copy-in and copy-out streams beside the compute
   // stream, ordering events (see run_pipelined).
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
-  static constexpr int kPipeEvents = 2 + 2 * 8 + 1;
+  // Second compute stream of the slab pipeline: consecutive slabs alternate
+  // between the context stream and this one, so the last wave of one slab's
+  // kernel shares the SMs with the first of the next.
+  cudaStream_t compute2 = nullptr;
+  static constexpr int kPipeEvents = 2 + 2 * 8 + 2;
   cudaEvent_t pev[kPipeEvents] = {};
 };
 
@@ -253,10 +258,10 @@ int ensure_work(t1m_context* ctx, size_t bytes) {
 
 // B-panel and operand-pack workspaces: both are optimisations, so a failed
 // allocation leaves the product on the in-kernel path instead of failing it.
-bool ensure_opt_work(t1m_context* ctx, void** buf, size_t* have, size_t bytes) {
+bool ensure_opt_work(cudaStream_t user, void** buf, size_t* have, size_t bytes) {
   if (*have >= bytes) return true;
   if (*buf) {
-    cudaStreamSynchronize(ctx->stream);
+    cudaStreamSynchronize(user);  // the only stream that uses this buffer
     cudaFree(*buf);
   }
   *buf = nullptr;
@@ -276,7 +281,7 @@ bool ensure_opt_work(t1m_context* ctx, void** buf, size_t* have, size_t bytes) {
 // kernel launch.  Adds the kernels it launched to *kernels.
 int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
                    const GemmArgs& g, cudaStream_t s, int* kernels, int* used_method,
-                   int* splits_out) {
+                   int* splits_out, int slot) {
   int nk = 0;
   int splits = 1;
   cudaError_t e = cudaSuccess;
@@ -319,13 +324,15 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
     } else {
       std::string err;
       int ran = method;
+      // Workspaces of this compute stream (slot 1: the pipeline's second).
       const size_t pb = tc_panel_bytes(dtype, gm.M, gm.N, gm.K);
-      const bool pan = pb > 0 && ensure_opt_work(ctx, &ctx->panel, &ctx->panel_bytes, pb);
+      const bool pan =
+          pb > 0 && ensure_opt_work(s, &ctx->panel[slot], &ctx->panel_bytes[slot], pb);
       const size_t kb = tc_pack_bytes(dtype, hp);
-      const bool pk = kb > 0 && ensure_opt_work(ctx, &ctx->pack, &ctx->pack_bytes, kb);
+      const bool pk = kb > 0 && ensure_opt_work(s, &ctx->pack[slot], &ctx->pack_bytes[slot], kb);
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
-                    pan ? ctx->panel : nullptr, pan ? ctx->panel_bytes : 0,
-                    pk ? ctx->pack : nullptr, pk ? ctx->pack_bytes : 0);
+                    pan ? ctx->panel[slot] : nullptr, pan ? ctx->panel_bytes[slot] : 0,
+                    pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0);
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -396,15 +403,18 @@ bool plan_slabs(const HostPlan& hp, size_t es, Slabs* sl) {
 
 namespace {
 
-// The slab pipeline (see plan_slabs).  Streams: copy_in (host->device),
-// the context stream (kernels), copy_out (device->host); events order them:
+// The slab pipeline (see plan_slabs).  Streams: copy_in (host->device), two
+// compute streams (the context stream for even slabs, compute2 for odd ones)
+// and copy_out (device->host); events order them:
 //   copy_in : [after earlier work on the context stream] resident operand,
 //             then per slab its range of the streamed operand (and of C when
 //             C is read) -> pev[2 + i]
-//   stream  : waits for the resident operand (pev[1]) and pev[2 + i], runs
-//             slab i -> pev[2 + kMaxSlabs + i]
+//   compute : waits for the resident operand (pev[1]) and pev[2 + i], runs
+//             slab i with its stream's own workspaces -> pev[2 + kMaxSlabs + i]
 //   copy_out: waits for pev[2 + kMaxSlabs + i], copies slab i of C back
-// The call returns once copy_out has finished (the result is in host memory).
+// Slabs are disjoint outputs, so the two compute streams may overlap.  The
+// call returns once copy_out and compute2 have finished (the result is in
+// host memory).
 int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
                   const GemmArgs& g0, const t1m_tensor* a, const t1m_tensor* b,
                   const t1m_tensor* c, const Slabs& sl, bool readC, bool timing,
@@ -421,6 +431,7 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   cudaEventRecord(ctx->pev[0], s);
   cudaStreamWaitEvent(ctx->copy_in, ctx->pev[0], 0);
   cudaStreamWaitEvent(ctx->copy_out, ctx->pev[0], 0);
+  cudaStreamWaitEvent(ctx->compute2, ctx->pev[0], 0);
   // Resident operand, whole.
   const int res = sl.along_n ? 0 : 1;
   const t1m_tensor* rt = sl.along_n ? a : b;
@@ -431,6 +442,7 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   h2d += static_cast<int64_t>(rbytes);
   cudaEventRecord(ctx->pev[1], ctx->copy_in);
   cudaStreamWaitEvent(s, ctx->pev[1], 0);
+  cudaStreamWaitEvent(ctx->compute2, ctx->pev[1], 0);
 
   const int xs = sl.along_n ? 1 : 0;
   const t1m_tensor* xt = sl.along_n ? b : a;
@@ -458,8 +470,12 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
         return cuda_fail(ctx, e, "copy C slab to device");
       h2d += static_cast<int64_t>(cn);
     }
+    // Slabs alternate between the two compute streams (independent outputs:
+    // the tail of one kernel overlaps the start of the next).
+    const int slot = i & 1;
+    cudaStream_t cs = slot ? ctx->compute2 : s;
     cudaEventRecord(ctx->pev[2 + i], ctx->copy_in);
-    cudaStreamWaitEvent(s, ctx->pev[2 + i], 0);
+    cudaStreamWaitEvent(cs, ctx->pev[2 + i], 0);
     // The slab as a contraction of its own: the slab dimension shortened
     // and the streamed operand and C shifted by its first index (uniform
     // strides, so no scatter vector changes).
@@ -478,9 +494,10 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
     }
     gs.k_per_split = hp.K;
     gs.c_split_stride = 0;
-    if (int st = launch_product(ctx, method, dtype, es, hp, gs, s, &kernels, &used_method, &splits))
+    if (int st = launch_product(ctx, method, dtype, es, hp, gs, cs, &kernels, &used_method,
+                                &splits, slot))
       return st;
-    cudaEventRecord(ctx->pev[2 + kMaxSlabs + i], s);
+    cudaEventRecord(ctx->pev[2 + kMaxSlabs + i], cs);
     cudaStreamWaitEvent(ctx->copy_out, ctx->pev[2 + kMaxSlabs + i], 0);
     if ((e = cudaMemcpyAsync(static_cast<char*>(c->data) + co,
                              static_cast<const char*>(ctx->stage[2]) + co, cn,
@@ -490,6 +507,8 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   }
   cudaEventRecord(ctx->pev[2 + 2 * kMaxSlabs], ctx->copy_out);
   cudaStreamWaitEvent(s, ctx->pev[2 + 2 * kMaxSlabs], 0);
+  cudaEventRecord(ctx->pev[3 + 2 * kMaxSlabs], ctx->compute2);
+  cudaStreamWaitEvent(s, ctx->pev[3 + 2 * kMaxSlabs], 0);
   if (timing) cudaEventRecord(ctx->ev[3], s);
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "contraction");
@@ -564,6 +583,7 @@ int t1m_create(t1m_context** out, int device) {
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->compute2, cudaStreamNonBlocking);
   for (int i = 0; i < t1m_context::kPipeEvents && e == cudaSuccess; ++i)
     e = cudaEventCreateWithFlags(&ctx->pev[i], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, 64);
@@ -595,8 +615,14 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->work) cudaFree(ctx->work);
-  if (ctx->panel) cudaFree(ctx->panel);
-  if (ctx->pack) cudaFree(ctx->pack);
+  for (int i = 0; i < 2; ++i) {
+    if (ctx->panel[i]) cudaFree(ctx->panel[i]);
+    if (ctx->pack[i]) cudaFree(ctx->pack[i]);
+  }
+  if (ctx->compute2) {
+    cudaStreamSynchronize(ctx->compute2);
+    cudaStreamDestroy(ctx->compute2);
+  }
   for (int i = 0; i < t1m_context::kPipeEvents; ++i)
     if (ctx->pev[i]) cudaEventDestroy(ctx->pev[i]);
   if (ctx->copy_in) {
@@ -828,7 +854,8 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     g.C = static_cast<char*>(g_all.C) + oc * static_cast<int64_t>(es);
     g.k_per_split = std::max<int64_t>(hp.K, 1);
     g.c_split_stride = 0;
-    if (int st = launch_product(ctx, method, dtype, es, hp, g, s, &kernels, &used_method, &splits))
+    if (int st = launch_product(ctx, method, dtype, es, hp, g, s, &kernels, &used_method, &splits,
+                                0))
       return st;
   }
   if (timing) cudaEventRecord(ctx->ev[2], s);
