@@ -71,7 +71,7 @@ struct t1m_context {
   // between the context stream and this one, so the last wave of one slab's
   // kernel shares the SMs with the first of the next.
   cudaStream_t compute2 = nullptr;
-  static constexpr int kPipeEvents = 2 + 2 * 8 + 2;
+  static constexpr int kPipeEvents = 3 + 8 + 2 * 8 + 2;
   cudaEvent_t pev[kPipeEvents] = {};
 };
 
@@ -404,17 +404,29 @@ bool plan_slabs(const HostPlan& hp, size_t es, Slabs* sl) {
 namespace {
 
 // The slab pipeline (see plan_slabs).  Streams: copy_in (host->device), two
-// compute streams (the context stream for even slabs, compute2 for odd ones)
-// and copy_out (device->host); events order them:
-//   copy_in : [after earlier work on the context stream] resident operand,
-//             then per slab its range of the streamed operand (and of C when
-//             C is read) -> pev[2 + i]
-//   compute : waits for the resident operand (pev[1]) and pev[2 + i], runs
-//             slab i with its stream's own workspaces -> pev[2 + kMaxSlabs + i]
-//   copy_out: waits for pev[2 + kMaxSlabs + i], copies slab i of C back
-// Slabs are disjoint outputs, so the two compute streams may overlap.  The
+// compute streams (the context stream and compute2, alternating) and
+// copy_out (device->host).  The resident operand (A for slabs along N, B for
+// slabs along M) goes first, in two halves along its other dimension when
+// each half is one 2-D region (unit stride there, uniform K stride): half 0,
+// the first two streamed slabs, half 1, the remaining slabs.  A block (slab
+// i, half h) is launched once its inputs are queued, on the next compute
+// stream (each with its own workspaces), and waits for them by events; C
+// slab i goes back once its blocks are done.  Blocks are disjoint outputs
+// and multiples of the output tile, so the two compute streams may overlap
+// and every output element is computed as on the device-buffer path.  The
 // call returns once copy_out and compute2 have finished (the result is in
 // host memory).
+enum : int {
+  kEvStart = 0,                      // earlier work on the context stream done
+  kEvRes = 1,                        // + h: resident operand half h on the device
+  kEvSlab = 3,                       // + i: streamed slab i (and its C range) on the device
+  kEvDone = kEvSlab + kMaxSlabs,     // + 2 i + h: block (i, h) computed
+  kEvOut = kEvDone + 2 * kMaxSlabs,  // copy_out finished
+  kEvC2 = kEvOut + 1,                // compute2 finished
+  kEvCount = kEvC2 + 1
+};
+static_assert(kEvCount <= t1m_context::kPipeEvents, "pipeline events");
+
 int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
                   const GemmArgs& g0, const t1m_tensor* a, const t1m_tensor* b,
                   const t1m_tensor* c, const Slabs& sl, bool readC, bool timing,
@@ -428,21 +440,39 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   int64_t h2d = 0, d2h = 0;
   if (timing) cudaEventRecord(ctx->ev[0], s);
   // Earlier work on the context stream may still use the staging buffers.
-  cudaEventRecord(ctx->pev[0], s);
-  cudaStreamWaitEvent(ctx->copy_in, ctx->pev[0], 0);
-  cudaStreamWaitEvent(ctx->copy_out, ctx->pev[0], 0);
-  cudaStreamWaitEvent(ctx->compute2, ctx->pev[0], 0);
-  // Resident operand, whole.
+  cudaEventRecord(ctx->pev[kEvStart], s);
+  cudaStreamWaitEvent(ctx->copy_in, ctx->pev[kEvStart], 0);
+  cudaStreamWaitEvent(ctx->copy_out, ctx->pev[kEvStart], 0);
+  cudaStreamWaitEvent(ctx->compute2, ctx->pev[kEvStart], 0);
+
+  // Resident operand and its halves: along N, A split along M (uA_m = 1,
+  // rows of K at stride uA_k); along M, B split along N likewise.
   const int res = sl.along_n ? 0 : 1;
   const t1m_tensor* rt = sl.along_n ? a : b;
   const size_t rbytes = sl.along_n ? bytesA : bytesB;
-  if ((e = cudaMemcpyAsync(ctx->stage[res], rt->data, rbytes, cudaMemcpyHostToDevice,
-                           ctx->copy_in)) != cudaSuccess)
-    return cuda_fail(ctx, e, "copy resident operand to device");
-  h2d += static_cast<int64_t>(rbytes);
-  cudaEventRecord(ctx->pev[1], ctx->copy_in);
-  cudaStreamWaitEvent(s, ctx->pev[1], 0);
-  cudaStreamWaitEvent(ctx->compute2, ctx->pev[1], 0);
+  const int64_t rlen = sl.along_n ? hp.M : hp.N;                 // the halved dimension
+  const int64_t ru = sl.along_n ? hp.uA_m : hp.uB_n;             // its stride in the operand
+  const int64_t rk = sl.along_n ? hp.uA_k : hp.uB_k;             // the operand's K stride
+  const int64_t cu = sl.along_n ? hp.uC_m : hp.uC_n;             // C's stride along it
+  const int64_t half = (rlen / 2 + 127) / 128 * 128;
+  int64_t kp = 0;
+  const bool split = ru == 1 && rk >= rlen && cu >= 1 && rlen >= 256 && half < rlen &&
+                     choose_splits(ctx, method, dtype, sl.along_n ? half : sl.width,
+                                   sl.along_n ? sl.width : half, hp.K, es, &kp) == 1;
+  const int halves = split ? 2 : 1;
+  auto copy_resident = [&](int h) -> cudaError_t {
+    if (!split) {
+      h2d += static_cast<int64_t>(rbytes);
+      return cudaMemcpyAsync(ctx->stage[res], rt->data, rbytes, cudaMemcpyHostToDevice,
+                             ctx->copy_in);
+    }
+    const int64_t lo = h * half, hi = h ? rlen : half;
+    const size_t off = size_t(lo) * es, width = size_t(hi - lo) * es, pitch = size_t(rk) * es;
+    h2d += static_cast<int64_t>(width) * hp.K;
+    return cudaMemcpy2DAsync(static_cast<char*>(ctx->stage[res]) + off, pitch,
+                             static_cast<const char*>(rt->data) + off, pitch, width,
+                             static_cast<size_t>(hp.K), cudaMemcpyHostToDevice, ctx->copy_in);
+  };
 
   const int xs = sl.along_n ? 1 : 0;
   const t1m_tensor* xt = sl.along_n ? b : a;
@@ -450,35 +480,37 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   // the device first, so copying the range back leaves them as they were.
   const bool c_in = readC || hp.spanC != hp.M * hp.N;
   const int64_t len = sl.along_n ? hp.N : hp.M;
-  int kernels = 0, used_method = method, splits = 1;
-  for (int i = 0; i < sl.count; ++i) {
+  auto copy_slab = [&](int i) -> cudaError_t {
     const int64_t lo = i * sl.width, hi = std::min(len, lo + sl.width);
-    // Streamed operand and C: element ranges of this slab.
     const int64_t x0 = lo * sl.ux + sl.x_lo, x1 = (hi - 1) * sl.ux + sl.x_hi + 1;
     const int64_t c0 = lo * sl.uc + sl.c_lo, c1 = (hi - 1) * sl.uc + sl.c_hi + 1;
     const size_t xo = size_t(x0) * es, xn = size_t(x1 - x0) * es;
     const size_t co = size_t(c0) * es, cn = size_t(c1 - c0) * es;
-    if ((e = cudaMemcpyAsync(static_cast<char*>(ctx->stage[xs]) + xo,
-                             static_cast<const char*>(xt->data) + xo, xn, cudaMemcpyHostToDevice,
-                             ctx->copy_in)) != cudaSuccess)
-      return cuda_fail(ctx, e, "copy slab to device");
+    cudaError_t r = cudaMemcpyAsync(static_cast<char*>(ctx->stage[xs]) + xo,
+                                    static_cast<const char*>(xt->data) + xo, xn,
+                                    cudaMemcpyHostToDevice, ctx->copy_in);
     h2d += static_cast<int64_t>(xn);
-    if (c_in) {
-      if ((e = cudaMemcpyAsync(static_cast<char*>(ctx->stage[2]) + co,
-                               static_cast<const char*>(c->data) + co, cn,
-                               cudaMemcpyHostToDevice, ctx->copy_in)) != cudaSuccess)
-        return cuda_fail(ctx, e, "copy C slab to device");
+    if (r == cudaSuccess && c_in) {
+      r = cudaMemcpyAsync(static_cast<char*>(ctx->stage[2]) + co,
+                          static_cast<const char*>(c->data) + co, cn, cudaMemcpyHostToDevice,
+                          ctx->copy_in);
       h2d += static_cast<int64_t>(cn);
     }
-    // Slabs alternate between the two compute streams (independent outputs:
-    // the tail of one kernel overlaps the start of the next).
-    const int slot = i & 1;
+    if (r == cudaSuccess) r = cudaEventRecord(ctx->pev[kEvSlab + i], ctx->copy_in);
+    return r;
+  };
+
+  int kernels = 0, used_method = method, splits = 1, nblock = 0;
+  // Block (slab i, half h): the slab dimension shortened to the slab, the
+  // halved dimension to the half, operands and C shifted accordingly
+  // (uniform strides, so no scatter vector changes).
+  auto launch_block = [&](int i, int h) -> int {
+    const int slot = nblock++ & 1;
     cudaStream_t cs = slot ? ctx->compute2 : s;
-    cudaEventRecord(ctx->pev[2 + i], ctx->copy_in);
-    cudaStreamWaitEvent(cs, ctx->pev[2 + i], 0);
-    // The slab as a contraction of its own: the slab dimension shortened
-    // and the streamed operand and C shifted by its first index (uniform
-    // strides, so no scatter vector changes).
+    cudaStreamWaitEvent(cs, ctx->pev[kEvRes + h], 0);
+    cudaStreamWaitEvent(cs, ctx->pev[kEvSlab + i], 0);
+    const int64_t lo = i * sl.width, hi = std::min(len, lo + sl.width);
+    const int64_t hlo = split ? h * half : 0, hhi = split ? (h ? rlen : half) : rlen;
     GemmArgs gs = g0;
     gs.A = ctx->stage[0];
     gs.B = ctx->stage[1];
@@ -487,28 +519,66 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
       gs.N = hi - lo;
       gs.B = static_cast<const char*>(gs.B) + size_t(lo * hp.uB_n) * es;
       gs.C = static_cast<char*>(gs.C) + size_t(lo * hp.uC_n) * es;
+      if (split) {
+        gs.M = hhi - hlo;
+        gs.A = static_cast<const char*>(gs.A) + size_t(hlo * hp.uA_m) * es;
+        gs.C = static_cast<char*>(gs.C) + size_t(hlo * hp.uC_m) * es;
+      }
     } else {
       gs.M = hi - lo;
       gs.A = static_cast<const char*>(gs.A) + size_t(lo * hp.uA_m) * es;
       gs.C = static_cast<char*>(gs.C) + size_t(lo * hp.uC_m) * es;
+      if (split) {
+        gs.N = hhi - hlo;
+        gs.B = static_cast<const char*>(gs.B) + size_t(hlo * hp.uB_n) * es;
+        gs.C = static_cast<char*>(gs.C) + size_t(hlo * hp.uC_n) * es;
+      }
     }
     gs.k_per_split = hp.K;
     gs.c_split_stride = 0;
     if (int st = launch_product(ctx, method, dtype, es, hp, gs, cs, &kernels, &used_method,
                                 &splits, slot))
       return st;
-    cudaEventRecord(ctx->pev[2 + kMaxSlabs + i], cs);
-    cudaStreamWaitEvent(ctx->copy_out, ctx->pev[2 + kMaxSlabs + i], 0);
-    if ((e = cudaMemcpyAsync(static_cast<char*>(c->data) + co,
-                             static_cast<const char*>(ctx->stage[2]) + co, cn,
-                             cudaMemcpyDeviceToHost, ctx->copy_out)) != cudaSuccess)
-      return cuda_fail(ctx, e, "copy C slab to host");
+    cudaEventRecord(ctx->pev[kEvDone + 2 * i + h], cs);
+    return T1M_OK;
+  };
+  auto copy_back = [&](int i) -> cudaError_t {
+    for (int h = 0; h < halves; ++h) cudaStreamWaitEvent(ctx->copy_out, ctx->pev[kEvDone + 2 * i + h], 0);
+    const int64_t lo = i * sl.width, hi = std::min(len, lo + sl.width);
+    const int64_t c0 = lo * sl.uc + sl.c_lo, c1 = (hi - 1) * sl.uc + sl.c_hi + 1;
+    const size_t co = size_t(c0) * es, cn = size_t(c1 - c0) * es;
     d2h += static_cast<int64_t>(cn);
+    return cudaMemcpyAsync(static_cast<char*>(c->data) + co,
+                           static_cast<const char*>(ctx->stage[2]) + co, cn,
+                           cudaMemcpyDeviceToHost, ctx->copy_out);
+  };
+
+  // Copies in order, each followed by the blocks it completes.
+  if ((e = copy_resident(0)) != cudaSuccess) return cuda_fail(ctx, e, "copy resident operand");
+  cudaEventRecord(ctx->pev[kEvRes], ctx->copy_in);
+  const int early = split ? std::min(2, sl.count) : 0;  // slabs before the second half
+  for (int i = 0; i < early; ++i) {
+    if ((e = copy_slab(i)) != cudaSuccess) return cuda_fail(ctx, e, "copy slab to device");
+    if (int st = launch_block(i, 0)) return st;
   }
-  cudaEventRecord(ctx->pev[2 + 2 * kMaxSlabs], ctx->copy_out);
-  cudaStreamWaitEvent(s, ctx->pev[2 + 2 * kMaxSlabs], 0);
-  cudaEventRecord(ctx->pev[3 + 2 * kMaxSlabs], ctx->compute2);
-  cudaStreamWaitEvent(s, ctx->pev[3 + 2 * kMaxSlabs], 0);
+  if (split) {
+    if ((e = copy_resident(1)) != cudaSuccess) return cuda_fail(ctx, e, "copy resident operand");
+    cudaEventRecord(ctx->pev[kEvRes + 1], ctx->copy_in);
+    for (int i = 0; i < early; ++i) {
+      if (int st = launch_block(i, 1)) return st;
+      if ((e = copy_back(i)) != cudaSuccess) return cuda_fail(ctx, e, "copy C slab to host");
+    }
+  }
+  for (int i = early; i < sl.count; ++i) {
+    if ((e = copy_slab(i)) != cudaSuccess) return cuda_fail(ctx, e, "copy slab to device");
+    for (int h = 0; h < halves; ++h)
+      if (int st = launch_block(i, h)) return st;
+    if ((e = copy_back(i)) != cudaSuccess) return cuda_fail(ctx, e, "copy C slab to host");
+  }
+  cudaEventRecord(ctx->pev[kEvOut], ctx->copy_out);
+  cudaStreamWaitEvent(s, ctx->pev[kEvOut], 0);
+  cudaEventRecord(ctx->pev[kEvC2], ctx->compute2);
+  cudaStreamWaitEvent(s, ctx->pev[kEvC2], 0);
   if (timing) cudaEventRecord(ctx->ev[3], s);
   e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "contraction");
