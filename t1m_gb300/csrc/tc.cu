@@ -2360,7 +2360,15 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   TcProblem p;
   if (!tc_prepare(args, plan, splits, &p)) return cudaErrorInvalidConfiguration;
   {
-    const bool pa = p.amode == kAGather && a_big;
+    // A per-16-row block-TMA operand A is packed as well when that puts the
+    // product on the one-tile kernel (B by TMA or by panels): the block form
+    // of the persistent kernel measured 3440 clocks per stage against 1450
+    // (abcd,ebfd->aecf at extents 32: 113 -> 79 us).  A block-mode B is left
+    // to the persistent kernel: without panels (few M tiles) the packed form
+    // measured slower (abcd,dbea->ec: 66 -> 75 us).
+    const bool a_blk = (p.block_maps & 1) != 0 || p.amode == kAMK16;
+    const bool b_blk = (p.block_maps & 2) != 0;
+    const bool pa = a_big && (p.amode == kAGather || (a_blk && (panels_ok || !b_blk)));
     const bool pb = p.bmode == kBGather && b_big && !panels_ok;
     if (pa || pb) {
       const int before = *kernels;

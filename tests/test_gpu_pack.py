@@ -140,3 +140,29 @@ def test_pack_auto_config2b(ctx, torch_cuda):
     got = gc.cpu().numpy()
     err = np.abs(got - ref).max() / np.abs(ref).max()
     assert err < 1e-6, err
+
+
+def test_pack_block_mode_a(ctx, torch_cuda):
+    """abcd,ebfd->aecf at extents 32 (the adjoint workload's product): A's
+    per-16-row block form is packed so the product runs on the one-tile
+    kernel with B from panels (pack, panel pass, product), and the automatic
+    method meets 1e-6 against FP64."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    ext = dict(a=32, b=32, c=32, d=32, e=32, f=32)
+    rng = np.random.default_rng(133)
+    la, lb, lc = "abcd", "ebfd", "aecf"
+    da, fa = _operand(rng, la, np.complex64, ext)
+    db, fb = _operand(rng, lb, np.complex64, ext)
+    dc = [ext[ch] for ch in lc]
+    ga, gb = torch.from_numpy(fa).cuda(), torch.from_numpy(fb).cuda()
+    gc = torch.zeros(int(np.prod(dc)), dtype=torch.complex64, device="cuda")
+    rep = t1m.contract_scaled(1.0, t1m.tensor(da, ga, t1m.col_major), la,
+                              t1m.tensor(db, gb, t1m.col_major), lb, 0.0,
+                              t1m.tensor(dc, gc, t1m.col_major), lc, ctx=ctx)
+    torch.cuda.synchronize()
+    assert rep.kernels == 3, rep.kernels
+    ref = _ref(la, lb, lc, fa, fb, da, db, dc).T.reshape(-1)
+    got = gc.cpu().numpy()
+    err = np.abs(got - ref).max() / np.abs(ref).max()
+    assert err < 1e-6, err
