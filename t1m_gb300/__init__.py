@@ -280,10 +280,10 @@ def _scalar_bytes(dtype: int, v) -> C.Array:
 def contract_raw(alpha, a: tensor, la: str, b: tensor, lb: str, beta, c: tensor, lc: str,
                  flags: int = 0, ctx: Context | None = None) -> Report:
     """One call of t1m_contract; returns its report."""
-    ctx = ctx or default_context()
     (pa, da), (pb, db), (pc, dc) = _data_ptr(a.data), _data_ptr(b.data), _data_ptr(c.data)
     if not da == db == dc:
         raise TypeError(f"mixed element types {(str(da), str(db), str(dc))}")
+    ctx = ctx or default_context()
     dtype = _DTYPE_OF[da]
     keep: list = []
     ta, tb, tc = a._c(keep, pa), b._c(keep, pb), c._c(keep, pc)
