@@ -281,7 +281,7 @@ bool ensure_opt_work(cudaStream_t user, void** buf, size_t* have, size_t bytes) 
 // kernel launch.  Adds the kernels it launched to *kernels.
 int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
                    const GemmArgs& g, cudaStream_t s, int* kernels, int* used_method,
-                   int* splits_out, int slot) {
+                   int* splits_out, int slot, bool allow_split) {
   int nk = 0;
   int splits = 1;
   cudaError_t e = cudaSuccess;
@@ -298,7 +298,10 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
                   std::string("method ") + std::to_string(method) +
                       " is not available for this dtype/contraction");
     int64_t kps = g.K;
-    splits = choose_splits(ctx, method, dtype, g.M, g.N, g.K, es, &kps);
+    // Blocks of the host-buffer pipeline never split: the whole product runs
+    // unsplit on the device-buffer path, and concurrent blocks must not share
+    // the split-K workspace.
+    splits = allow_split ? choose_splits(ctx, method, dtype, g.M, g.N, g.K, es, &kps) : 1;
     // Split-K: the main kernel writes raw partial products (alpha = 1,
     // beta = 0) into dense workspace slices, m fastest; the reduction sums
     // them in FP64 and applies the epilogue.
@@ -455,10 +458,7 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   const int64_t rk = sl.along_n ? hp.uA_k : hp.uB_k;             // the operand's K stride
   const int64_t cu = sl.along_n ? hp.uC_m : hp.uC_n;             // C's stride along it
   const int64_t half = (rlen / 2 + 127) / 128 * 128;
-  int64_t kp = 0;
-  const bool split = ru == 1 && rk >= rlen && cu >= 1 && rlen >= 256 && half < rlen &&
-                     choose_splits(ctx, method, dtype, sl.along_n ? half : sl.width,
-                                   sl.along_n ? sl.width : half, hp.K, es, &kp) == 1;
+  const bool split = ru == 1 && rk >= rlen && cu >= 1 && rlen >= 256 && half < rlen;
   const int halves = split ? 2 : 1;
   auto copy_resident = [&](int h) -> cudaError_t {
     if (!split) {
@@ -537,7 +537,7 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
     gs.k_per_split = hp.K;
     gs.c_split_stride = 0;
     if (int st = launch_product(ctx, method, dtype, es, hp, gs, cs, &kernels, &used_method,
-                                &splits, slot))
+                                &splits, slot, false))
       return st;
     cudaEventRecord(ctx->pev[kEvDone + 2 * i + h], cs);
     return T1M_OK;
@@ -925,7 +925,7 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     g.k_per_split = std::max<int64_t>(hp.K, 1);
     g.c_split_stride = 0;
     if (int st = launch_product(ctx, method, dtype, es, hp, g, s, &kernels, &used_method, &splits,
-                                0))
+                                0, true))
       return st;
   }
   if (timing) cudaEventRecord(ctx->ev[2], s);

@@ -65,3 +65,34 @@ def test_pipelined_strided_c_keeps_gaps(ctx, torch_cuda):
     t1m.contract_scaled(1.0, v(ga), "ik", v(gb), "kj", 0.0, v(gc), "ij", ctx=ctx)
     torch.cuda.synchronize()
     np.testing.assert_array_equal(Cv, gc.cpu().numpy())
+
+
+@pytest.mark.parametrize("method", ["tc_3xtf32", "tc_bf16x6"])
+def test_pipelined_narrow_last_slab(ctx, torch_cuda, method):
+    """Row-major M = 2624, N = 1024, K = 6144: four slabs along M of 768 rows
+    (96 tiles: the pipeline runs), the last 320 rows (40 tiles), each slab in
+    two halves of B along N on alternating compute streams.  The last slab's
+    blocks would split K on their own; pipeline blocks never split, so they
+    stay bit-identical to the device path and never share the split-K
+    workspace."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    rng = np.random.default_rng(62)
+    M, N, K = 2624, 1024, 6144
+    A = _rand(rng, M * K, np.complex64).reshape(M, K)
+    B = _rand(rng, K * N, np.complex64).reshape(K, N)
+    C = np.zeros((M, N), np.complex64)
+    v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+    ctx.set_method(method)
+    try:
+        rep = t1m.contract_scaled(1.0, v(A), "mk", v(B), "kn", 0.0, v(C), "mn", ctx=ctx)
+        ga, gb = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+        gc = torch.zeros((M, N), dtype=torch.complex64, device="cuda")
+        dev = t1m.contract_scaled(1.0, v(ga), "mk", v(gb), "kn", 0.0, v(gc), "mn", ctx=ctx)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_method("auto")
+    # 4 slabs x 2 halves (plus a panel pass per block for 3xTF32).
+    assert rep.kernels >= 8 and rep.split_k == 1 and dev.split_k == 1, rep.kernels
+    assert rep.h2d_bytes >= A.nbytes + B.nbytes and rep.d2h_bytes == C.nbytes
+    np.testing.assert_array_equal(C, gc.cpu().numpy())
