@@ -38,6 +38,8 @@ LA, LB, LC = "ijkl", "klmn", "ijmn"
 M = N = K = EXT * EXT
 FLOPS = 8.0 * M * N * K
 WORKLOAD = "complex64 ijkl,klmn->ijmn, all extents 64 (M=N=K=4096), col-major"
+# One metric string for both arms, so their lines compare directly.
+METRIC = "complex TFLOP/s (8MNK/t) tensor-core vs plain GPU form @ rel err <=1e-6 vs FP64"
 
 
 def _dist():
@@ -200,7 +202,7 @@ def run_reference(args) -> None:
     total = sum(times)
     value = flops * len(times) / total / 1e12
     line = {
-        "impl": "reference", "metric": "complex TFLOP/s (8MNK/t)", "value": value,
+        "impl": "reference", "metric": METRIC, "value": value,
         "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / len(times), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "complex64", "data": "synthetic (U[-1,1] re/im, seed 1)",
@@ -366,7 +368,7 @@ def run_gpu(args) -> None:
             peak = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
             peak_note = "FP32 SIMT nominal 152 SM x 128 lanes x 2 x max SM clock"
         line = {
-            "metric": "complex TFLOP/s (8MNK/t) tensor-core vs plain GPU form @ rel err <=1e-6 vs FP64",
+            "metric": METRIC,
             "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
@@ -534,6 +536,45 @@ def workload_logmag(args):
           flush=True)
 
 
+def workload_c128(args):
+    """Precision form, complex128 companion: ijkl,klmn->ijmn extents 64
+    (M = N = K = 4096) in FP64, on the FP64 tensor cores (DMMA) and on the
+    plain FP64 kernel (the automatic choice), with sampled FP64 errors and
+    the fraction of the nominal FP64 peak (no measured FP64 peak exists)."""
+    import torch
+    import t1m_gb300 as t1m
+    ctx = t1m.Context()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev)
+    g.manual_seed(1234)
+    mk = lambda n: torch.complex(  # noqa: E731
+        torch.rand(n, device=dev, generator=g, dtype=torch.float64) * 2 - 1,
+        torch.rand(n, device=dev, generator=g, dtype=torch.float64) * 2 - 1)
+    ga, gb = mk(M * K), mk(K * N)
+    gc = torch.zeros(M * N, dtype=torch.complex128, device=dev)
+    dims = [[EXT] * 4] * 3
+    ta, tb, tc = (t1m.tensor(d, x) for d, x in zip(dims, (ga, gb, gc)))
+    # GB300's nominal dense FP64 rate (its FP64 units are a small fraction
+    # of the FP32 ones; no measured FP64 peak exists).
+    peak = 1.25
+    out = []
+    for m in ("dmma", "auto"):
+        ctx.set_method(m)
+        rep = t1m.contract_raw(1.0, ta, LA, tb, LB, 0.0, tc, LC, 0, ctx)
+        err = _sampled_err(LA, LB, LC, dims, ga, gb, gc, samples=256)
+        ms = _events_ms(torch, lambda: t1m.contract_raw(1.0, ta, LA, tb, LB, 0.0, tc, LC,
+                                                        t1m.FLAG_NO_TIMING, ctx),
+                        max(1, min(args.steps, 3)), 1)
+        out.append({"method": m, "ran": t1m.method(rep.method).name, "split_k": rep.split_k,
+                    "ms": ms, "tflops": FLOPS / ms / 1e9, "frac_of_fp64_nominal": FLOPS / ms / 1e9 / peak,
+                    "rel_err_max": err[0], "rel_err_fro": err[1]})
+    ctx.close()
+    print(json.dumps({"workload": "config3 complex128 companion, ijkl,klmn->ijmn extents 64 "
+                                  "(M=N=K=4096), col-major", "fp64_peak_nominal_tflops": peak,
+                      "cases": out}), flush=True)
+
+
 def workload_batch(args):
     """Batching form: 1024 updates xay,asb->xsyb then xsyb,ytb->xst with
     x, y, a, b ~ U{16..256 step 16}, s, t ~ U{2, 4}, components N(0, 1/sqrt(bond));
@@ -648,7 +689,7 @@ def main() -> None:
     ap.add_argument("--method", default="auto")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="headline",
-                    choices=["headline", "config2", "logmag", "batch", "vjp"])
+                    choices=["headline", "config2", "logmag", "c128", "batch", "vjp"])
     ap.add_argument("--items", type=int, default=1024)
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch workload: heuristic kernel families instead of the autotuner")
@@ -662,7 +703,7 @@ def main() -> None:
         # with torch events; a created stream (not the legacy stream 0, which
         # t1m_set_stream reads as "the context's own") keeps both on one.
         import torch
-        fn = {"config2": workload_config2, "logmag": workload_logmag,
+        fn = {"config2": workload_config2, "logmag": workload_logmag, "c128": workload_c128,
               "batch": workload_batch, "vjp": workload_vjp}[args.workload]
         with torch.cuda.stream(torch.cuda.Stream()):
             fn(args)

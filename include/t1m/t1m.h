@@ -107,6 +107,10 @@ class context {
   context& operator=(const context&) = delete;
 
   void set_method(t1m_method m) { check(t1m_set_method(h_, m)); }
+  /// Number of K partitions (0 = automatic).
+  void set_split_k(int splits) { check(t1m_set_split_k(h_, splits)); }
+  /// Cap on each optional tensor-core workspace in bytes (-1 = none, 0 = off).
+  void set_workspace_limit(int64_t bytes) { check(t1m_set_workspace_limit(h_, bytes)); }
   /// Run on a caller-owned cudaStream_t (nullptr = the context's own stream).
   void set_stream(void* stream) { check(t1m_set_stream(h_, stream)); }
   void synchronize() { check(t1m_synchronize(h_)); }

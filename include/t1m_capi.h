@@ -60,7 +60,9 @@ typedef enum t1m_layout {
 /* How the contraction is computed on the GPU.  The reference always runs the
  * BLIS real micro-kernel on 1M-packed panels (t1m.h:508-554, mappings.h:91-99). */
 typedef enum t1m_method {
-  T1M_METHOD_AUTO = 0,       /* pick per dtype and shape                     */
+  T1M_METHOD_AUTO = 0,       /* pick per dtype and shape; FP32 partials are
+                                kept short enough for 1e-6 against FP64 (K
+                                split, partials and epilogue in FP64)        */
   T1M_METHOD_PLAIN = 1,      /* SIMT FP32/FP64 FMA (the plain GPU form)      */
   T1M_METHOD_TC_3XTF32 = 2,  /* complex64: tcgen05 kind::tf32, hi/lo split,
                                 3 products, FP32 accumulation in TMEM         */
@@ -91,8 +93,25 @@ typedef struct t1m_report {
   int64_t h2d_bytes;
   int64_t d2h_bytes;
   int32_t kernels;     /* kernels launched by this call                     */
-  int32_t reserved;
+  int32_t path;        /* tensor-core products: T1M_PATH_* code of the last
+                          product (how its operands were fetched); 0 for
+                          the plain and FP64 kernels                         */
 } t1m_report;
+
+/* t1m_report.path: bit 12 marks a tensor-core product; bits 0-3 the fetch
+ * mode of A, bits 4-7 that of B; bit 8 the persistent kernel (else one tile
+ * per CTA); bits 9/10 A/B densely repacked first (then loaded by TMA).
+ * A modes: 0 gathered, 1 one TMA box [k][m], 2 TMA boxes per 16-row block of
+ * unit-stride rows, 3 one TMA box [m][k], 4 per 16-row block with unit-stride
+ * K, 5 per 16-row block and 16-K block (adjoint operands).
+ * B modes: 0 gathered, 1 one TMA box [n][k], 2 one box [k][n], 3 per 16-column
+ * block with unit-stride K, 4 per 16-column block and 16-K block (adjoint
+ * operands), 5 B split once beforehand into panels (loaded by TMA). */
+#define T1M_PATH_TC 0x1000
+#define T1M_PATH_PERSISTENT 0x100
+#define T1M_PATH_A_PACKED 0x200
+#define T1M_PATH_B_PACKED 0x400
+#define T1M_PATH_B_PANELS 5
 
 typedef struct t1m_context t1m_context;
 
@@ -118,6 +137,15 @@ int t1m_set_method(t1m_context* ctx, int method);
  * the GPU).  The reference streams K in KC chunks inside one thread
  * (t1m.h:512-548); this is its parallel counterpart. */
 int t1m_set_split_k(t1m_context* ctx, int splits);
+/* Cap, in bytes, on each optional workspace of the tensor-core products: B
+ * split once into panels, and dense repacks of operands that would otherwise
+ * be gathered element by element.  Products whose workspace would exceed it
+ * run without (same results, bit for bit; only speed changes).  -1 (the
+ * default) = no cap, 0 = never use them.  For callers with a tight device
+ * memory budget; the split-K workspace is not optional and not capped here.
+ * No reference counterpart (the reference packs into one aligned_alloc'ed
+ * buffer per call, t1m.h:450-460). */
+int t1m_set_workspace_limit(t1m_context* ctx, int64_t bytes);
 int t1m_synchronize(t1m_context* ctx);
 const char* t1m_status_string(int status);
 const char* t1m_last_error(const t1m_context* ctx);
@@ -209,7 +237,8 @@ int t1m_group_destroy(t1m_group* group);
  *   - all calls share the one scratch array and each overwrites it: calls that
  *     overlap on the GPU (other host threads or streams) race;
  *   - the first call on a device looks up the scratch address; make that call
- *     before any stream capture.
+ *     before any stream capture.  The address is kept for the life of the
+ *     process: calls after cudaDeviceReset are not supported.
  * On failure a message is written to err (err_len bytes, may be 0). */
 #define T1M_NOALLOC_SCRATCH_BYTES (64u << 20)
 int t1m_contract_noalloc(void* stream, int method, int dtype, const void* alpha,

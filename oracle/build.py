@@ -5,8 +5,9 @@
   baseline call on every machine).
 * ``oracle/_ref/libt1m_ref.so`` — the UNMODIFIED reference headers instantiated
   through ``oracle/ref_shim.cpp`` against the BLIS stand-in.  Built only where
-  the reference source tree exists (``T1M_REFERENCE_DIR``, default
-  ``/root/reference``); it is never committed and never needed at run time.
+  the reference source tree exists (``T1M_REFERENCE_DIR``, default: a
+  ``reference`` directory beside this repository's root); it is never
+  committed and never needed at run time.
 
 Both use ``-ffp-contract=off`` and explicit ``std::fma`` in the micro-kernel so
 x86-64 and aarch64 builds produce the same bits.
@@ -24,7 +25,9 @@ SHIM_SRC = HERE / "ref_shim.cpp"
 STANDIN = HERE / "standin"
 PORT_LIB = HERE / "_build" / "libt1m_port.so"
 REF_LIB = HERE / "_ref" / "libt1m_ref.so"
-REFERENCE_DIR = Path(os.environ.get("T1M_REFERENCE_DIR", "/root/reference"))
+# The reference checkout: $T1M_REFERENCE_DIR, else a sibling of the repo root.
+REFERENCE_DIR = Path(os.environ.get("T1M_REFERENCE_DIR",
+                                    str(HERE.parent.parent / "reference")))
 
 CXXFLAGS = ["-O3", "-fPIC", "-shared", "-ffp-contract=off", "-Wall"]
 

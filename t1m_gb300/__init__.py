@@ -46,6 +46,12 @@ FLAG_CONJ_B = 4
 FLAG_NO_TIMING = 8
 
 
+# t1m_report.path (T1M_PATH_* of t1m_capi.h)
+PATH_TC, PATH_PERSISTENT, PATH_A_PACKED, PATH_B_PACKED = 0x1000, 0x100, 0x200, 0x400
+A_MODES = {0: "gather", 1: "MK", 2: "MK16", 3: "KM", 4: "KM16", 5: "MK16K"}
+B_MODES = {0: "gather", 1: "NK", 2: "KN", 3: "NK16", 4: "KN16", 5: "panels"}
+
+
 class memory_layout(enum.IntEnum):
     """Same values as the reference's enum (t1m.h:29)."""
     row_major = 0
@@ -83,10 +89,21 @@ class Report(C.Structure):
                 ("n", C.c_int64), ("k", C.c_int64), ("flops", C.c_double),
                 ("kernel_ms", C.c_double), ("h2d_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("kernels", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("path", C.c_int32)]
 
     def as_dict(self) -> dict:
-        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+    @property
+    def fetch(self) -> dict | None:
+        """How the last tensor-core product fetched its operands (decoded
+        t1m_report.path; None for the plain and FP64 kernels)."""
+        p = self.path
+        if not p & PATH_TC:
+            return None
+        return {"a": A_MODES[p & 15], "b": B_MODES[(p >> 4) & 15],
+                "persistent": bool(p & PATH_PERSISTENT), "a_packed": bool(p & PATH_A_PACKED),
+                "b_packed": bool(p & PATH_B_PACKED)}
 
 
 class PlanInfo(C.Structure):
@@ -123,6 +140,7 @@ def lib() -> C.CDLL:
         h.t1m_set_stream.argtypes = [vp, vp]
         h.t1m_set_method.argtypes = [vp, i32]
         h.t1m_set_split_k.argtypes = [vp, i32]
+        h.t1m_set_workspace_limit.argtypes = [vp, C.c_int64]
         h.t1m_synchronize.argtypes = [vp]
         h.t1m_status_string.restype = C.c_char_p
         h.t1m_status_string.argtypes = [i32]
@@ -163,6 +181,11 @@ class Context:
     def set_split_k(self, splits: int) -> None:
         """Force the number of K partitions (0 = automatic)."""
         self._check(lib().t1m_set_split_k(self._h, int(splits)))
+
+    def set_workspace_limit(self, nbytes: int) -> None:
+        """Cap each optional tensor-core workspace (B panels, dense operand
+        packs); -1 = no cap, 0 = never use them (results are unchanged)."""
+        self._check(lib().t1m_set_workspace_limit(self._h, int(nbytes)))
 
     def set_stream(self, stream: int | None) -> None:
         self._check(lib().t1m_set_stream(self._h, stream or None))

@@ -63,6 +63,10 @@ struct t1m_context {
   void* pack[2] = {nullptr, nullptr};
   size_t pack_bytes[2] = {0, 0};
   int split_k = 0;
+  // Cap on each optional workspace (panels, packs); -1 = none.
+  int64_t opt_work_limit = -1;
+  // T1M_PATH_* code of the last tensor-core product of the current call.
+  int last_path = 0;
   int num_sms = 152;
   // Host-operand pipeline: copy-in and copy-out streams beside the compute
   // stream, ordering events (see run_pipelined).
@@ -74,6 +78,28 @@ struct t1m_context {
   static constexpr int kPipeEvents = 3 + 8 + 2 * 8 + 2;
   cudaEvent_t pev[kPipeEvents] = {};
 };
+
+namespace t1m {
+namespace gb300 {
+
+int auto_method(int dtype, const HostPlan& plan) {
+  if ((dtype == T1M_COMPLEX64 || dtype == T1M_FLOAT32) && tc_supported(kMethodTcAuto, dtype, plan) &&
+      plan.M * plan.N * plan.K >= int64_t(1) << (dtype == T1M_FLOAT32 ? 20 : 18))
+    return kMethodTcAuto;
+  return T1M_METHOD_PLAIN;
+}
+
+int64_t accuracy_k_limit(int method, int dtype) {
+  const bool cplx = dtype == T1M_COMPLEX64;
+  if (dtype != T1M_COMPLEX64 && dtype != T1M_FLOAT32) return 0;
+  if (method == T1M_METHOD_PLAIN) return cplx ? 128 : 256;
+  if (method == kMethodTcAuto || method == T1M_METHOD_TC_3XTF32 || method == T1M_METHOD_TC_BF16X6)
+    return cplx ? 4096 : 8192;
+  return 0;
+}
+
+}  // namespace gb300
+}  // namespace t1m
 
 namespace {
 
@@ -196,12 +222,7 @@ int check_device_error(t1m_context* ctx) {
 }
 
 int choose_method(const t1m_context* ctx, int dtype, const HostPlan& plan) {
-  int m = ctx->method;
-  if (m != T1M_METHOD_AUTO) return m;
-  if ((dtype == T1M_COMPLEX64 || dtype == T1M_FLOAT32) && tc_supported(kMethodTcAuto, dtype, plan) &&
-      plan.M * plan.N * plan.K >= int64_t(1) << (dtype == T1M_FLOAT32 ? 20 : 18))
-    return kMethodTcAuto;
-  return T1M_METHOD_PLAIN;
+  return ctx->method != T1M_METHOD_AUTO ? ctx->method : auto_method(dtype, plan);
 }
 
 // Workspace cap of split-K (bytes of partial products).
@@ -211,8 +232,11 @@ constexpr size_t kMaxWorkBytes = size_t(2) << 30;
 // has too few tiles, each split keeping at least four K-steps; forced by
 // t1m_set_split_k.  Returns the split count and its K length (a multiple of
 // the kernel's K-step).
+// Under T1M_METHOD_AUTO (`promote`) the split count is also at least
+// ceil(K / accuracy_k_limit), so every FP32 partial stays within the 1e-6
+// error bound and the partials are summed in FP64.
 int choose_splits(const t1m_context* ctx, int method, int dtype, int64_t M, int64_t N,
-                  int64_t K, size_t elem, int64_t* k_per_split) {
+                  int64_t K, size_t elem, int64_t* k_per_split, bool promote = false) {
   int bm, bn, bk, per_sm;
   if (method == T1M_METHOD_PLAIN) {
     simt_tile(dtype, &bm, &bn, &bk);
@@ -233,6 +257,8 @@ int choose_splits(const t1m_context* ctx, int method, int dtype, int64_t M, int6
     const int64_t target = int64_t(ctx->num_sms) * per_sm;
     if (tiles < target / 2 && ksteps >= 8)
       s = std::min<int64_t>((target + tiles - 1) / tiles, ksteps / 4);
+    const int64_t lim = promote ? accuracy_k_limit(method, dtype) : 0;
+    if (lim > 0) s = std::max<int64_t>(s, (K + lim - 1) / lim);
   }
   s = std::max<int64_t>(1, std::min<int64_t>({s, ksteps, 4096}));
   while (s > 1 && size_t(s) * size_t(M) * size_t(N) * elem > kMaxWorkBytes) --s;
@@ -301,7 +327,9 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
     // Blocks of the host-buffer pipeline never split: the whole product runs
     // unsplit on the device-buffer path, and concurrent blocks must not share
     // the split-K workspace.
-    splits = allow_split ? choose_splits(ctx, method, dtype, g.M, g.N, g.K, es, &kps) : 1;
+    splits = allow_split ? choose_splits(ctx, method, dtype, g.M, g.N, g.K, es, &kps,
+                                         ctx->method == T1M_METHOD_AUTO)
+                         : 1;
     // Split-K: the main kernel writes raw partial products (alpha = 1,
     // beta = 0) into dense workspace slices, m fastest; the reduction sums
     // them in FP64 and applies the epilogue.
@@ -328,14 +356,19 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       std::string err;
       int ran = method;
       // Workspaces of this compute stream (slot 1: the pipeline's second).
+      const auto within = [&](size_t bytes) {
+        return ctx->opt_work_limit < 0 || bytes <= static_cast<size_t>(ctx->opt_work_limit);
+      };
       const size_t pb = tc_panel_bytes(dtype, gm.M, gm.N, gm.K);
-      const bool pan =
-          pb > 0 && ensure_opt_work(s, &ctx->panel[slot], &ctx->panel_bytes[slot], pb);
+      const bool pan = pb > 0 && within(pb) &&
+                       ensure_opt_work(s, &ctx->panel[slot], &ctx->panel_bytes[slot], pb);
       const size_t kb = tc_pack_bytes(dtype, hp);
-      const bool pk = kb > 0 && ensure_opt_work(s, &ctx->pack[slot], &ctx->pack_bytes[slot], kb);
+      const bool pk = kb > 0 && within(kb) &&
+                      ensure_opt_work(s, &ctx->pack[slot], &ctx->pack_bytes[slot], kb);
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
                     pan ? ctx->panel[slot] : nullptr, pan ? ctx->panel_bytes[slot] : 0,
-                    pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0);
+                    pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0,
+                    &ctx->last_path);
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -595,6 +628,7 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
     report->h2d_bytes = h2d;
     report->d2h_bytes = d2h;
     report->kernels = kernels;
+    report->path = ctx->last_path;
     if (timing) {
       // Copies and kernels overlap: the whole call is reported as kernel time.
       float t = 0;
@@ -665,6 +699,12 @@ int t1m_create(t1m_context** out, int device) {
   ctx->stream = ctx->own_stream;
   ctx->num_sms = prop.multiProcessorCount;
   *out = ctx;
+  return T1M_OK;
+}
+
+int t1m_set_workspace_limit(t1m_context* ctx, int64_t bytes) {
+  if (!ctx || bytes < -1) return T1M_ERR_INVALID_ARGUMENT;
+  ctx->opt_work_limit = bytes;
   return T1M_OK;
 }
 
@@ -793,6 +833,7 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "strided tensor without strides");
   cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "set device");
+  ctx->last_path = 0;
 
   // Plan (cached).
   const std::string key = plan_key(dtype, a, sa, la, b, sb, lb, c, sc, lc);
@@ -875,7 +916,8 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     int64_t kps = 0;
     const int64_t sm = sl.along_n ? hp.M : sl.width, sn = sl.along_n ? sl.width : hp.N;
     if (method == T1M_METHOD_PLAIN || method == T1M_METHOD_DMMA || tc_supported(method, dtype, hp))
-      if (choose_splits(ctx, method, dtype, sm, sn, hp.K, es, &kps) == 1)
+      if (choose_splits(ctx, method, dtype, sm, sn, hp.K, es, &kps,
+                        ctx->method == T1M_METHOD_AUTO) == 1)
         return run_pipelined(ctx, method, dtype, es, hp, g, a, b, c, sl, readC, timing, report);
   }
 
@@ -953,6 +995,7 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     report->h2d_bytes = h2d;
     report->d2h_bytes = d2h;
     report->kernels = kernels;
+    report->path = ctx->last_path;
     if (timing) {
       float t01 = 0, t12 = 0, t23 = 0;
       cudaEventElapsedTime(&t01, ctx->ev[0], ctx->ev[1]);
@@ -1005,6 +1048,7 @@ extern "C" int t1m_contract_vjp(t1m_context* ctx, int dtype, const t1m_tensor* d
       report->h2d_bytes = r1.h2d_bytes + r2.h2d_bytes;
       report->d2h_bytes = r1.d2h_bytes + r2.d2h_bytes;
       report->kernels = r1.kernels + r2.kernels;
+      report->path = r2.path;
     }
   }
   return T1M_OK;
@@ -1044,7 +1088,16 @@ int group_splits(int dtype, int fam, const HostPlan& hp, size_t es, int64_t* k_p
     if (fam == kFamSimtSkinny) bk = 16;
   }
   const int64_t ksteps = std::max<int64_t>(1, (hp.K + bk - 1) / bk);
-  const int64_t cap_steps = std::max<int64_t>(1, kGroupKCap / bk);
+  // Families are chosen by the library, so the AUTO precision rule applies:
+  // plain tiles accumulate sequentially and cover at most its K limit (the
+  // skinny kernel's lanes each sum a 1/32 share, the tensor-core limit is
+  // above the cap).
+  int64_t cap = kGroupKCap;
+  if (fam == kFamSimt) {
+    const int64_t lim = accuracy_k_limit(T1M_METHOD_PLAIN, dtype);
+    if (lim > 0) cap = std::min(cap, lim);
+  }
+  const int64_t cap_steps = std::max<int64_t>(1, cap / bk);
   int64_t s = (ksteps + cap_steps - 1) / cap_steps;
   s = std::max<int64_t>(1, std::min<int64_t>(s, 4096));
   while (s > 1 && size_t(s) * size_t(hp.M) * size_t(hp.N) * es > kGroupItemWorkBytes) --s;

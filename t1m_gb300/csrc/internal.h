@@ -125,6 +125,25 @@ constexpr int kSkinnyAsyncMaxK = 1024;
 // 3xTF32 elsewhere); the report carries the method that ran.
 constexpr int kMethodTcAuto = 100;
 
+// Method of T1M_METHOD_AUTO for a planned contraction (capi.cu): the tensor
+// cores (kMethodTcAuto) for complex64 with M*N*K >= 2^18 and float32 with
+// M*N*K >= 2^20, else the plain kernel.  t1m_contract and
+// t1m_contract_noalloc share it.
+int auto_method(int dtype, const HostPlan& plan);
+
+// Precision rule of T1M_METHOD_AUTO: the longest K range (elements of the
+// contracted bundle) one FP32-accumulated partial product may cover so that
+// its relative error against FP64 stays below 1e-6 (0: no limit, the FP64
+// paths).  Longer contractions are split along K and the partials summed,
+// with the epilogue, in FP64 (the split-K reduction).
+//  * plain FP32: sequential FMA accumulation, error ~3.1e-8 sqrt(terms)
+//    (measured 2.8e-6 at 8192 real terms): 256 real terms per partial, i.e.
+//    K <= 128 complex or 256 real;
+//  * tensor cores: the correction accumulator truncates ~2e-8 per MMA over
+//    the whole range (4e-7 at K = 4096 complex): K <= 4096 complex or 8192
+//    real.
+int64_t accuracy_k_limit(int method, int dtype);
+
 // Launchers.  Return cudaError_t of the launch.
 // simt.cu: plain FP32/FP64 kernel; `splits` CTA rows along K.
 cudaError_t launch_simt(int dtype, const GemmArgs& args, int splits, cudaStream_t stream,
@@ -183,10 +202,12 @@ cudaError_t launch_splitk_reduce_group(int dtype, const SplitReduce* dev, int n,
 // panels, at least tc_panel_bytes(dtype, M, N, K) bytes, or null.
 // `pack` (pack_bytes) is workspace for operands repacked densely
 // (tc_pack_bytes), or null.
+// `path` (may be null) receives the product's T1M_PATH_* code (t1m_capi.h).
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel = nullptr,
-                      size_t panel_bytes = 0, void* pack = nullptr, size_t pack_bytes = 0);
+                      size_t panel_bytes = 0, void* pack = nullptr, size_t pack_bytes = 0,
+                      int* path = nullptr);
 // Panel workspace a product would use (0: panels not used at this size).
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K);
 // Pack workspace a product may use (0: neither operand would be packed).

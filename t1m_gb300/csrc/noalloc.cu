@@ -23,7 +23,8 @@
 //    stream before returning), so consecutive calls from one thread do not.
 //  * The first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture.
+//    before any stream capture.  The address is kept for the life of the
+//    process, so calls after cudaDeviceReset are not supported.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -194,12 +195,14 @@ extern "C" int t1m_contract_noalloc(void* stream_ptr, int method, int dtype, con
   e = cudaMemsetAsync(err_word, 0, sizeof(int), stream);
   if (e != cudaSuccess) return finish(err, err_len, T1M_ERR_CUDA, cudaGetErrorString(e));
 
-  // Method as t1m_contract's automatic choice, or the one asked for.
+  // The method asked for, or t1m_contract's automatic choice (the same rule,
+  // auto_method).  Its tensor-core form picks BF16x6 or 3xTF32 per operand
+  // layout exactly as t1m_contract does; only the B panels and dense operand
+  // packs, which would need workspace, are not used here (they change
+  // speed, not results).
   const bool cplx = dtype == T1M_COMPLEX64 || dtype == T1M_COMPLEX128;
-  if (method == T1M_METHOD_AUTO)
-    method = (dtype == T1M_COMPLEX64 && hp.M * hp.N * hp.K >= int64_t(1) << 18)
-                 ? T1M_METHOD_TC_3XTF32
-                 : T1M_METHOD_PLAIN;
+  const bool is_auto = method == T1M_METHOD_AUTO;
+  if (is_auto) method = auto_method(dtype, hp);
   const bool dmma_ok = method == T1M_METHOD_DMMA && (dtype == T1M_FLOAT64 || dtype == T1M_COMPLEX128);
   if (method != T1M_METHOD_PLAIN && !dmma_ok && !tc_supported(method, dtype, hp))
     return finish(err, err_len, T1M_ERR_UNSUPPORTED, "method not available for this dtype");
@@ -259,7 +262,10 @@ extern "C" int t1m_contract_noalloc(void* stream_ptr, int method, int dtype, con
     const int64_t target = int64_t(sms) * per_sm;
     if (tiles < target / 2 && ksteps >= 8)
       s = std::min<int64_t>((target + tiles - 1) / tiles, ksteps / 4);
-    s = std::max<int64_t>(1, std::min<int64_t>(s, ksteps));
+    // The precision rule of the automatic method (accuracy_k_limit).
+    const int64_t lim = is_auto ? accuracy_k_limit(method, dtype) : 0;
+    if (lim > 0) s = std::max<int64_t>(s, (hp.K + lim - 1) / lim);
+    s = std::max<int64_t>(1, std::min<int64_t>({s, ksteps, 4096}));
     const size_t room = T1M_NOALLOC_SCRATCH_BYTES - fixed;
     while (s > 1 && size_t(s) * size_t(hp.M) * size_t(hp.N) * es > room) --s;
     const int64_t steps_per = (ksteps + s - 1) / s;

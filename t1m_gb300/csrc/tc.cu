@@ -2231,9 +2231,21 @@ size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel, size_t panel_bytes,
-                      void* pack, size_t pack_bytes) {
+                      void* pack, size_t pack_bytes, int* path) {
   *kernels = 0;
   if (used_method) *used_method = method;
+  if (path) *path = 0;
+  // The report's path code: fetch modes in TcProblem's numbering, B panels
+  // as T1M_PATH_B_PANELS, kernel form and packed operands as flag bits.
+  auto set_path = [&](int am, int bm, bool persistent, bool pa, bool pb) {
+    if (path)
+      *path = T1M_PATH_TC | am | (bm << 4) | (persistent ? T1M_PATH_PERSISTENT : 0) |
+              (pa ? T1M_PATH_A_PACKED : 0) | (pb ? T1M_PATH_B_PACKED : 0);
+  };
+  auto one_tile_a = [](int am) { return am == kTmaMK ? kAMK : am == kTmaKM ? kAKM : kAGather; };
+  auto one_tile_b = [](int bm) {
+    return bm == kTmaNK ? kBNK : bm == kTmaKN ? kBKN : bm == kPanelNK ? T1M_PATH_B_PANELS : kBGather;
+  };
   if (!tc_supported(method, dtype, plan)) {
     *err = "tensor-core method not available for this dtype";
     return cudaErrorNotSupported;
@@ -2355,6 +2367,8 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                     static_cast<unsigned>(splits));
     const cudaError_t e = launch_prec<true>(method, am, bm, gr, maps, stream, err_flag, grid);
     if (e == cudaSuccess) ++*kernels;
+    set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A,
+             packed_args.B != args.B);
     return e;
   }
   TcProblem p;
@@ -2413,8 +2427,11 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     if (panels)
       if ((e = use_panels(p.g, &maps, &bm)) != cudaSuccess) return e;
     e = launch_prec<false>(method, am, bm, p.g, maps, stream, err_flag, grid);
+    set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A,
+             packed_args.B != args.B);
   } else {
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
+    set_path(p.amode, p.bmode, true, packed_args.A != args.A, packed_args.B != args.B);
   }
   if (e == cudaSuccess) ++*kernels;
   return e;

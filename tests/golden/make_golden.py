@@ -1,7 +1,7 @@
 """Generate the committed golden fixtures from the reference itself.
 
 Run in a checkout where the reference tree exists (``T1M_REFERENCE_DIR``,
-default /root/reference):
+default: a ``reference`` directory beside this repository's root):
 
     python tests/golden/make_golden.py
 
@@ -34,7 +34,8 @@ sys.path.insert(0, str(ROOT))
 from oracle import libs  # noqa: E402
 from oracle import numpy_oracle as no  # noqa: E402
 
-REF = Path(os.environ.get("T1M_REFERENCE_DIR", "/root/reference"))
+REF = Path(os.environ.get("T1M_REFERENCE_DIR",
+                          str(Path(__file__).resolve().parents[3] / "reference")))
 OUT = Path(__file__).resolve().parent
 
 
