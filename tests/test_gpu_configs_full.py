@@ -114,7 +114,12 @@ def test_config5_adjoint_full_size(ctx, torch_cuda, cfg5, method, workspace):
 
 def test_config5_adjoint_finite_differences(ctx, torch_cuda, cfg5):
     """Directional central differences (step 1e-6) of the complex128 loss
-    L = Re sum conj(dC) * (A*B) against the complex64 adjoint's gradients."""
+    L = Re sum conj(dC) * (A*B) against the complex64 adjoint's gradients.
+
+    Along the FP64 gradient itself the derivative is |grad|^2 (no
+    cancellation), so it is held to 1e-6 relative.  Along a random direction
+    V the derivative is a sum of a million terms of either sign; there the
+    normwise bound |<dA - grad, V>| <= 1e-6 |grad| |V| applies."""
     import t1m_gb300 as t1m
     torch = torch_cuda
     A, B, G, _, _ = cfg5
@@ -123,22 +128,33 @@ def test_config5_adjoint_finite_differences(ctx, torch_cuda, cfg5):
     t1m.contract_vjp(_rows(torch, G), lc, _rows(torch, A), la, _rows(torch, B), lb,
                      _rows(torch, dA), _rows(torch, dB), ctx=ctx)
     a, b, gc = (z.to(torch.complex128) for z in (A, B, G))
+    grad_a = torch.einsum("aecf,ebfd->abcd", gc, b.conj())
+    grad_b = torch.einsum("abcd,aecf->ebfd", a.conj(), gc)
 
     def loss(x, y):
         return torch.sum(torch.conj(gc) * torch.einsum("abcd,ebfd->aecf", x, y)).real.item()
 
     gen = torch.Generator(device="cuda")
     gen.manual_seed(13)
+
+    def rand_dir():
+        return torch.complex(
+            torch.rand(a.shape, device="cuda", generator=gen, dtype=torch.float64) * 2 - 1,
+            torch.rand(a.shape, device="cuda", generator=gen, dtype=torch.float64) * 2 - 1)
+
     h = 1e-6
-    for _ in range(2):
-        V = torch.complex(torch.rand(a.shape, device="cuda", generator=gen, dtype=torch.float64),
-                          torch.rand(a.shape, device="cuda", generator=gen, dtype=torch.float64))
-        fd_a = (loss(a + h * V, b) - loss(a - h * V, b)) / (2 * h)
-        fd_b = (loss(a, b + h * V) - loss(a, b - h * V)) / (2 * h)
-        an_a = torch.sum(torch.conj(dA.to(torch.complex128)) * V).real.item()
-        an_b = torch.sum(torch.conj(dB.to(torch.complex128)) * V).real.item()
-        assert abs(fd_a - an_a) <= TOL * abs(an_a), (fd_a, an_a)
-        assert abs(fd_b - an_b) <= TOL * abs(an_b), (fd_b, an_b)
+    for va, vb, along in ((grad_a, grad_b, True), (rand_dir(), rand_dir(), False)):
+        fd_a = (loss(a + h * va, b) - loss(a - h * va, b)) / (2 * h)
+        fd_b = (loss(a, b + h * vb) - loss(a, b - h * vb)) / (2 * h)
+        an_a = torch.sum(torch.conj(dA.to(torch.complex128)) * va).real.item()
+        an_b = torch.sum(torch.conj(dB.to(torch.complex128)) * vb).real.item()
+        if along:
+            bound_a, bound_b = TOL * abs(an_a), TOL * abs(an_b)
+        else:
+            bound_a = TOL * (torch.linalg.vector_norm(grad_a) * torch.linalg.vector_norm(va)).item()
+            bound_b = TOL * (torch.linalg.vector_norm(grad_b) * torch.linalg.vector_norm(vb)).item()
+        assert abs(fd_a - an_a) <= bound_a, (along, fd_a, an_a)
+        assert abs(fd_b - an_b) <= bound_b, (along, fd_b, an_b)
 
 
 # ------------------------------------------------------------ precision ---
@@ -245,8 +261,10 @@ def _sweep_batch(torch, n_items, seed=2024):
 @pytest.mark.slow
 def test_config4_full_batch_grouped_graph(ctx, torch_cuda):
     """All 1024 updates (2048 contractions) as one grouped launch under a CUDA
-    graph with the autotuner; every item's outputs checked on a sampled row
-    of R (all y, b of one x, s) and of O (all t of one x, s) against FP64."""
+    graph with the autotuner; every item's outputs checked against FP64 on
+    sampled rows: R[x, s, :, :] (all y, b of one x, s) and O[x, :, :] for
+    four x (all s, t; O rows hold only 2-4 entries, too few to normalise
+    the error by on their own)."""
     import t1m_gb300 as t1m
     torch = torch_cuda
     items, keep = _sweep_batch(torch, 1024)
@@ -258,18 +276,22 @@ def test_config4_full_batch_grouped_graph(ctx, torch_cuda):
     finally:
         grp.close()
     rng = np.random.default_rng(17)
-    worst = 0.0
+    worst = (0.0, None)
     c128 = torch.complex128
     for i, (X1, X2, X3, R, O) in enumerate(keep):
         x, s = int(rng.integers(X1.shape[0])), int(rng.integers(X2.shape[1]))
-        # R[x, s, :, :] = X1[x]^T X2[:, s, :];  O[x, s, :] = sum_yb R[x, s] X3.
+        # R[x, s, :, :] = X1[x]^T X2[:, s, :]
         r_ref = X1[x].to(c128).t() @ X2[:, s, :].to(c128)
-        o_ref = torch.einsum("yb,ytb->t", r_ref, X3.to(c128))
-        for got, ref in ((R[x, s], r_ref), (O[x, s], o_ref)):
+        xs = torch.from_numpy(rng.integers(0, X1.shape[0], 4)).cuda()
+        o_ref = torch.einsum("xsyb,ytb->xst",
+                             torch.einsum("xay,asb->xsyb", X1[xs].to(c128), X2.to(c128)),
+                             X3.to(c128))
+        for name, got, ref in (("R", R[x, s], r_ref), ("O", O[xs], o_ref)):
             e = ((got.to(c128) - ref).abs().max() / ref.abs().max()).item()
-            assert e == e, (i, "unwritten output (NaN)")
-            worst = max(worst, e)
-    assert worst <= TOL, worst
+            assert e == e, (i, name, "unwritten output (NaN)")
+            if e > worst[0]:
+                worst = (e, (i, name, tuple(X1.shape), tuple(X2.shape), tuple(X3.shape)))
+    assert worst[0] <= TOL, worst
 
 
 # -------------------------------------------------------- precision rule ---
