@@ -244,6 +244,7 @@ def run_gpu(args) -> None:
     import t1m_gb300 as t1m
 
     ctx = t1m.Context(local)
+    ctx.set_tile_form(args.tile_form)
     dev = torch.device("cuda", local)
     g = torch.Generator(device=dev)
     g.manual_seed(1234 + rank)
@@ -373,7 +374,8 @@ def run_gpu(args) -> None:
             "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
             "data": "synthetic (re/im U[-1,1], torch seed 1234+rank)",
-            "config": {"workload": WORKLOAD, "method": tc_method,
+            "config": {"workload": WORKLOAD, "method": tc_method, "tile_form": args.tile_form,
+                       "tile_path": rep0.fetch,
                        "l2": "inputs larger than L2 (A, B, C 134 MB each)",
                        "parallelism": f"replicas x{world}"},
             "plain_fp32": {"value": plain_tflops, "unit": "TFLOP/s", "steps": plain_steps,
@@ -687,6 +689,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--method", default="auto")
+    ap.add_argument("--tile-form", default="auto", choices=["auto", "one", "pair"],
+                    help="tensor-core tile form (one tile per CTA or CTA pairs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "config2", "logmag", "c128", "batch", "vjp"])

@@ -101,6 +101,7 @@ typedef struct t1m_report {
 /* t1m_report.path: bit 12 marks a tensor-core product; bits 0-3 the fetch
  * mode of A, bits 4-7 that of B; bit 8 the persistent kernel (else one tile
  * per CTA); bits 9/10 A/B densely repacked first (then loaded by TMA).
+ * Bit 11 (T1M_PATH_PAIR): clusters of two CTAs share each MMA.
  * A modes: 0 gathered, 1 one TMA box [k][m], 2 TMA boxes per 16-row block of
  * unit-stride rows, 3 one TMA box [m][k], 4 per 16-row block with unit-stride
  * K, 5 per 16-row block and 16-K block (adjoint operands).
@@ -108,6 +109,7 @@ typedef struct t1m_report {
  * block with unit-stride K, 4 per 16-column block and 16-K block (adjoint
  * operands), 5 B split once beforehand into panels (loaded by TMA). */
 #define T1M_PATH_TC 0x1000
+#define T1M_PATH_PAIR 0x800       /* CTA pairs (tcgen05 cta_group::2)        */
 #define T1M_PATH_PERSISTENT 0x100
 #define T1M_PATH_A_PACKED 0x200
 #define T1M_PATH_B_PACKED 0x400
@@ -146,6 +148,16 @@ int t1m_set_split_k(t1m_context* ctx, int splits);
  * No reference counterpart (the reference packs into one aligned_alloc'ed
  * buffer per call, t1m.h:450-460). */
 int t1m_set_workspace_limit(t1m_context* ctx, int64_t bytes);
+/* Tile form of single tensor-core contractions (complex64).  T1M_TILE_PAIR
+ * runs clusters of two CTAs whose MMAs (tcgen05 cta_group::2, 256 x 128 real
+ * tiles) each read half of B from either CTA, where both operands load by
+ * TMA; T1M_TILE_ONE keeps one 128 x 128 tile per CTA; T1M_TILE_AUTO (the
+ * default) picks pairs where they apply.  The reference's counterpart is
+ * BLIS's choice of micro-tile and cache blocking (bli/mappings.h:101-142). */
+#define T1M_TILE_AUTO 0
+#define T1M_TILE_ONE 1
+#define T1M_TILE_PAIR 2
+int t1m_set_tile_form(t1m_context* ctx, int form);
 int t1m_synchronize(t1m_context* ctx);
 const char* t1m_status_string(int status);
 const char* t1m_last_error(const t1m_context* ctx);

@@ -48,6 +48,9 @@ FLAG_NO_TIMING = 8
 
 # t1m_report.path (T1M_PATH_* of t1m_capi.h)
 PATH_TC, PATH_PERSISTENT, PATH_A_PACKED, PATH_B_PACKED = 0x1000, 0x100, 0x200, 0x400
+PATH_PAIR = 0x800
+# t1m_set_tile_form
+TILE_FORMS = {"auto": 0, "one": 1, "pair": 2}
 A_MODES = {0: "gather", 1: "MK", 2: "MK16", 3: "KM", 4: "KM16", 5: "MK16K"}
 B_MODES = {0: "gather", 1: "NK", 2: "KN", 3: "NK16", 4: "KN16", 5: "panels"}
 
@@ -102,7 +105,8 @@ class Report(C.Structure):
         if not p & PATH_TC:
             return None
         return {"a": A_MODES[p & 15], "b": B_MODES[(p >> 4) & 15],
-                "persistent": bool(p & PATH_PERSISTENT), "a_packed": bool(p & PATH_A_PACKED),
+                "persistent": bool(p & PATH_PERSISTENT), "pair": bool(p & PATH_PAIR),
+                "a_packed": bool(p & PATH_A_PACKED),
                 "b_packed": bool(p & PATH_B_PACKED)}
 
 
@@ -141,6 +145,7 @@ def lib() -> C.CDLL:
         h.t1m_set_method.argtypes = [vp, i32]
         h.t1m_set_split_k.argtypes = [vp, i32]
         h.t1m_set_workspace_limit.argtypes = [vp, C.c_int64]
+        h.t1m_set_tile_form.argtypes = [vp, i32]
         h.t1m_synchronize.argtypes = [vp]
         h.t1m_status_string.restype = C.c_char_p
         h.t1m_status_string.argtypes = [i32]
@@ -186,6 +191,13 @@ class Context:
         """Cap each optional tensor-core workspace (B panels, dense operand
         packs); -1 = no cap, 0 = never use them (results are unchanged)."""
         self._check(lib().t1m_set_workspace_limit(self._h, int(nbytes)))
+
+    def set_tile_form(self, form: int | str) -> None:
+        """Tile form of tensor-core products: "auto", "one" (one tile per
+        CTA) or "pair" (clusters of two CTAs sharing each MMA)."""
+        if isinstance(form, str):
+            form = TILE_FORMS[form]
+        self._check(lib().t1m_set_tile_form(self._h, int(form)))
 
     def set_stream(self, stream: int | None) -> None:
         self._check(lib().t1m_set_stream(self._h, stream or None))

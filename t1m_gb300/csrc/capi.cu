@@ -65,6 +65,8 @@ struct t1m_context {
   int split_k = 0;
   // Cap on each optional workspace (panels, packs); -1 = none.
   int64_t opt_work_limit = -1;
+  // T1M_TILE_* form of tensor-core products.
+  int tile_form = T1M_TILE_AUTO;
   // T1M_PATH_* code of the last tensor-core product of the current call.
   int last_path = 0;
   int num_sms = 152;
@@ -368,7 +370,7 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
                     pan ? ctx->panel[slot] : nullptr, pan ? ctx->panel_bytes[slot] : 0,
                     pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0,
-                    &ctx->last_path);
+                    &ctx->last_path, ctx->tile_form);
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -699,6 +701,12 @@ int t1m_create(t1m_context** out, int device) {
   ctx->stream = ctx->own_stream;
   ctx->num_sms = prop.multiProcessorCount;
   *out = ctx;
+  return T1M_OK;
+}
+
+int t1m_set_tile_form(t1m_context* ctx, int form) {
+  if (!ctx || form < T1M_TILE_AUTO || form > T1M_TILE_PAIR) return T1M_ERR_INVALID_ARGUMENT;
+  ctx->tile_form = form;
   return T1M_OK;
 }
 

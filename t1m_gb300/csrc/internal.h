@@ -207,7 +207,7 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel = nullptr,
                       size_t panel_bytes = 0, void* pack = nullptr, size_t pack_bytes = 0,
-                      int* path = nullptr);
+                      int* path = nullptr, int form = 0 /* T1M_TILE_* */);
 // Panel workspace a product would use (0: panels not used at this size).
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K);
 // Pack workspace a product may use (0: neither operand would be packed).

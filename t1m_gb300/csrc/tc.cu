@@ -1187,18 +1187,36 @@ static_assert(kAK1 % 4 == 0 && kMC1 % 32 == 0 && kBP1 >= 1 && kB16P1 >= 1, "conv
 // same 128-byte swizzle rows), the raw A stage doubles to 16 KB, B's raw
 // bytes are the complex layout's (k pairs for complex elements), and the
 // epilogue writes one real row per thread.
-template <bool kReal, bool kPanel>
+// CTA pairs (kPair): each CTA holds half of the B tile (64 columns), raw and
+// converted, so its B stages are half as large.
+// Both forms keep the same TMEM layout and pipeline: two chunk
+// accumulators (ping-pong), the corrections, two converted A stages.  A
+// 4-stage A ring with a single chunk accumulator measured slower in both
+// (the MMA thread then waits for each fold before a chunk's main products).
+constexpr int kBarrierBytes1 = 256;
+template <bool kReal, bool kPanel, bool kPair = false>
 constexpr int smem_bytes_1() {
-  return 1024 + kRaw * ((kReal ? 16384 : kRawABytes) + (kPanel ? 0 : kRawBBytes)) +
-         (kPanel ? kPanelStages : kStages) * kOpBytes + kBarrierBytes;
+  return 1024 +
+         kRaw * ((kReal ? 16384 : kRawABytes) + (kPanel ? 0 : (kPair ? kRawBBytes / 2 : kRawBBytes))) +
+         (kPanel ? kPanelStages : kStages) * (kPair ? kOpBytes / 2 : kOpBytes) + kBarrierBytes1;
 }
 
-template <int AMode, int BMode, int Prec, bool kReal>
+// kPair: clusters of two CTAs sharing one tcgen05.mma.cta_group::2 per
+// product (M = 256 real rows = 128 complex rows per pair, N = 128).  Each CTA
+// loads and converts its own 64 complex rows of A into its own TMEM, as in
+// the one-CTA form, but only its half of the B tile (64 columns), and the
+// pair's MMAs read B half from each CTA: per SM, half the B bytes staged,
+// converted and read by the tensor cores per flop.  One thread of the even
+// CTA issues every MMA; the converters of both CTAs arrive on its barriers,
+// and its commits arrive on the barriers of both.
+template <int AMode, int BMode, int Prec, bool kReal, bool kPair>
 __global__ void __launch_bounds__(kThreads1, 1)
 tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
   constexpr bool kBF16 = Prec != kPrecTF32x3;
   constexpr int kPieces = Prec == kPrecBF16x6 ? 3 : 2;
-  constexpr uint32_t kIdescP = kBF16 ? ptx::idesc_f32acc(1u /*BF16*/, 128, kTileN) : kIdesc;
+  // MMA M: 128 real rows per CTA, 256 for a pair.
+  constexpr uint32_t kIdescT = ptx::idesc_f32acc(kBF16 ? 1u /*BF16*/ : 2u /*TF32*/,
+                                                 kPair ? 256u : 128u, kTileN);
   constexpr bool kTmaA = AMode != kGatherMK;
   constexpr bool kPanel = BMode == kPanelNK;
   constexpr bool kTmaB = BMode == kTmaNK || BMode == kTmaKN;
@@ -1209,18 +1227,31 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   constexpr int kStepKE = kReal ? 32 : kStepK;         // K elements per stage
   constexpr int kCx = kReal ? 1 : 2;                   // floats per element (TMA coordinates)
   constexpr int kRawABytesT = kReal ? 16384 : kRawABytes;
-  constexpr int kRawBytesT = kRawABytesT + (kPanel ? 0 : kRawBBytes);
+  // B columns this CTA loads and converts, and the sizes that follow.
+  constexpr int kNCta = kPair ? kTileN / 2 : kTileN;
+  constexpr int kRawBBytesT = kNCta * kStepK * 8;
+  constexpr int kBHalfT = kNCta * 128;      // one converted B buffer (hi, lo or 2 pieces)
+  constexpr int kOpBytesT = 2 * kBHalfT;
+  constexpr int kBPT = (kNCta * kStepK / 2) / kConverters1;    // 16-byte TF32 B pieces per thread
+  constexpr int kB16PT = (kNCta * kStepK / 4) / kConverters1;  // bf16 B chunks per thread
+  static_assert(kBPT >= 1 && kB16PT >= 1, "B conversion split");
+  static_assert(!kPair || (!kReal && !kPanel && kTmaA && kTmaB),
+                "CTA pairs take complex operands loaded by TMA");
+  // Arrivals on the barriers the MMA thread waits for: the converter warps
+  // of this CTA, or of both CTAs of a pair.
+  constexpr uint32_t kConvArrivals = (kPair ? 2u : 1u) * (kConverters1 / 32);
+  constexpr int kRawBytesT = kRawABytesT + (kPanel ? 0 : kRawBBytesT);
   // Arrivals per raw stage: one expect_tx arrive from the TMA thread, one
   // cp.async completion arrive per gather thread.
   constexpr uint32_t kRawArrivals = (kTmaA || kTmaB ? 1u : 0u) + (kGather ? kLoaders : 0u);
-  constexpr uint32_t kTmaBytes = (kTmaA ? kRawABytesT : 0) + (kTmaB ? kRawBBytes : 0);
+  constexpr uint32_t kTmaBytes = (kTmaA ? kRawABytesT : 0) + (kTmaB ? kRawBBytesT : 0);
 
   extern __shared__ __align__(16) uint8_t smem_raw[];
   const uint32_t base = (ptx::smem_u32(smem_raw) + 1023u) & ~1023u;
   uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
-  const uint32_t raw0 = base;                          // kRaw x (A | B 16 KB)
-  const uint32_t op0 = raw0 + kRaw * kRawBytesT;       // kStages x (B hi | B lo)
-  const uint32_t bars = op0 + kOpStages * kOpBytes;
+  const uint32_t raw0 = base;                          // kRaw x (A | B)
+  const uint32_t op0 = raw0 + kRaw * kRawBytesT;       // kOpStages x (B hi | B lo)
+  const uint32_t bars = op0 + kOpStages * kOpBytesT;
   auto raw_a = [&](int r) { return raw0 + r * kRawBytesT; };
   auto raw_b = [&](int r) { return raw0 + r * kRawBytesT + kRawABytesT; };
   auto raw_full = [&](int r) { return bars + 8u * r; };
@@ -1234,16 +1265,22 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   // Panel stages: filled by TMA (one expect_tx arrive), emptied by an MMA commit.
   auto pfull = [&](int i) { return acc_bar + 16u + 8u * i; };
   auto pempty = [&](int i) { return acc_bar + 16u + 8u * (kPanelStages + i); };
-  static_assert(8 * (2 * kRaw + 2 * kStages + 5 + 1 + 2 * kPanelStages) <= kBarrierBytes,
+  static_assert(8 * (2 * kRaw + 2 * kStages + 5 + 1 + 2 * kPanelStages) <= kBarrierBytes1,
                 "barrier area");
   volatile uint32_t* tmem_slot_ptr = reinterpret_cast<volatile uint32_t*>(base_ptr + (tmem_slot - base));
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
+  const uint32_t rank = kPair ? ptx::cluster_ctarank() : 0u;
 
   if (warp == 0) {
-    ptx::tmem_alloc(tmem_slot, kTmemCols);
-    ptx::tmem_relinquish();
+    if constexpr (kPair) {
+      ptx::tmem_alloc2(tmem_slot, kTmemCols);
+      ptx::tmem_relinquish2();
+    } else {
+      ptx::tmem_alloc(tmem_slot, kTmemCols);
+      ptx::tmem_relinquish();
+    }
   }
   if (tid == 32) {
     if (kPanel) {
@@ -1257,12 +1294,12 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       ptx::mbar_init(raw_empty(r), kConverters1 / 32);
     }
     for (int s = 0; s < kStages; ++s) {
-      ptx::mbar_init(full_bar(s), kConverters1 / 32);
+      ptx::mbar_init(full_bar(s), kConvArrivals);
       ptx::mbar_init(empty_bar(s), 1);
     }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(chunk_full(b), 1);
-      ptx::mbar_init(chunk_empty(b), kConverters1 / 32);
+      ptx::mbar_init(chunk_empty(b), kConvArrivals);
     }
     ptx::mbar_init(acc_bar, 1);
     ptx::fence_mbar_init();
@@ -1271,31 +1308,56 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     if (kTmaA) ptx::tma_prefetch_desc(&maps.a);
     if (kTmaB) ptx::tma_prefetch_desc(&maps.b);
   }
+  // A pair starts once both CTAs have their barriers and TMEM.
   ptx::tc_fence_before();
-  __syncthreads();
+  if constexpr (kPair) ptx::cluster_sync(); else __syncthreads();
   ptx::tc_fence_after();
   const uint32_t tmem = *tmem_slot_ptr;
+  // Waits of the MMA thread (for a pair, the converters of both CTAs arrive
+  // on them), its MMAs and commits.
+  auto wait_conv = [&](uint32_t bar, uint32_t ph) { return ptx::mbar_wait(bar, ph); };
+  auto mma_tf = [&](uint32_t d, uint32_t a, uint64_t b, uint32_t acc) {
+    if constexpr (kPair) ptx::mma_tf32_ts2(d, a, b, kIdescT, acc);
+    else ptx::mma_tf32_ts(d, a, b, kIdescT, acc);
+  };
+  auto mma_bf = [&](uint32_t d, uint32_t a, uint64_t b, uint32_t acc) {
+    if constexpr (kPair) ptx::mma_f16_ts2(d, a, b, kIdescT, acc);
+    else ptx::mma_f16_ts(d, a, b, kIdescT, acc);
+  };
+  auto commit = [&](uint32_t bar) {
+    if constexpr (kPair) ptx::mma_commit2(bar);
+    else ptx::mma_commit(bar);
+  };
+  // Converter arrivals on the MMA thread's barriers (the even CTA's for a pair).
+  auto arrive_mma = [&](uint32_t bar) {
+    if constexpr (kPair) ptx::mbar_arrive_cluster(ptx::mapa(bar, 0));
+    else ptx::mbar_arrive(bar);
+  };
 
   const int64_t M = args.M, N = args.N;
   // Split-K: this CTA row covers K range [kb, K) (kb a multiple of kStepK).
   const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
   const int64_t K = min(args.K, kb + args.k_per_split);
-  const int64_t tiles_m = (M + kRowsT - 1) / kRowsT;
+  // Output tiles: kRowsT rows per CTA, two CTAs' rows per pair.
+  constexpr int kRowsTile = kPair ? 2 * kRowsT : kRowsT;
+  const int64_t tiles_m = (M + kRowsTile - 1) / kRowsTile;
   const int64_t tiles_n = (N + kTileN - 1) / kTileN;
-  // Groups of 16 M-tiles sweep N so CTAs running together share B in L2.
-  constexpr int64_t G = 16;
-  const int64_t t = blockIdx.x;
+  // Groups of 16 M-tiles of 64 rows (8 pair tiles) sweep N so CTAs running
+  // together share B in L2.
+  constexpr int64_t G = kPair ? 8 : 16;
+  const int64_t t = kPair ? (blockIdx.x >> 1) : blockIdx.x;
   const int64_t group = t / (G * tiles_n);
   const int64_t first_m = group * G;
   const int64_t gsize = min(G, tiles_m - first_m);
   const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
   const int64_t tn = (t % (G * tiles_n)) / gsize;
-  const int64_t m0 = tm * kRowsT, n0 = tn * kTileN;
+  const int64_t m0 = tm * kRowsTile + rank * kRowsT, n0 = tn * kTileN;
+  const int64_t nb0 = n0 + rank * kNCta;  // first B column this CTA loads
   const int64_t ksteps = (K - kb + kStepKE - 1) / kStepKE;
 
   if (warp == 0) {
     // ---------------------------------------------------------- MMA issue ---
-    if (lane == 0) {
+    if (lane == 0 && rank == 0) {
       for (int64_t s = 0; s < ksteps; ++s) {
         const int st = static_cast<int>(s % kStages);
         const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
@@ -1303,11 +1365,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         const int buf = static_cast<int>(c & 1);
         const bool chunk_start = (s % kFold) == 0;
         if (chunk_start && c >= 2 &&
-            !ptx::mbar_wait(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
+            !wait_conv(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
           record_error(err_flag, kErrChunkWait);
           break;
         }
-        if (!ptx::mbar_wait(full_bar(st), ph)) {
+        if (!wait_conv(full_bar(st), ph)) {
           record_error(err_flag, kErrFullWait);
           break;
         }
@@ -1319,47 +1381,51 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         ptx::tc_fence_after();
         const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
         const uint32_t d_corr = tmem + kCorrCol;
-        if constexpr (!kBF16) {
-          const uint32_t a_hi = tmem + kAStageCol + 64u * st;
-          const uint32_t a_lo = a_hi + 32u;
-          const uint32_t b_hi = op0 + sb * kOpBytes;
-          const uint32_t b_lo = b_hi + kBHalfBytes;
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk) {
-            const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
-            const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
-            ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
-            ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
-            ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
-          }
-        } else {
-          // A piece p: 16 TMEM columns at +16p; B piece p: 64-byte half
-          // (p & 1) of the rows of B buffer (p >> 1).  K = 16 per MMA.
-          const uint32_t a0 = tmem + kAStageCol + 64u * st;
-          const uint32_t bb = op0 + sb * kOpBytes;
-#pragma unroll
-          for (int kk = 0; kk < 2; ++kk) {
-            auto bd = [&](int p) {
-              return ptx::smem_desc_sw128(bb + (p >> 1) * kBHalfBytes + 64u * (p & 1) + 32u * kk);
-            };
-            const uint32_t ak = a0 + 8u * kk;
-            ptx::mma_f16_ts(d_main, ak, bd(0), kIdescP, (chunk_start && kk == 0) ? 0u : 1u);
-            ptx::mma_f16_ts(d_corr, ak, bd(1), kIdescP, (s == 0 && kk == 0) ? 0u : 1u);
-            ptx::mma_f16_ts(d_corr, ak + 16u, bd(0), kIdescP, 1u);
+        const uint32_t a_st = tmem + kAStageCol + 64u * st;
+        const uint32_t bb = op0 + sb * kOpBytesT;
+        // One stage: TF32x3 (kind::tf32, K = 8): 4 x (hi.hi -> main, hi.lo +
+        // lo.hi -> corrections).  bf16 (kind::f16, K = 16): A piece p at 16
+        // TMEM columns +16p, B piece p in 64-byte half (p & 1) of B buffer
+        // (p >> 1); 2 x (x0y0 -> main, x0y1 + x1y0 [+ x1y1 + x0y2 + x2y0] ->
+        // corrections).
+        auto bd = [&](int p, int kk) {
+          return ptx::smem_desc_sw128(bb + (p >> 1) * kBHalfT + 64u * (p & 1) + 32u * kk);
+        };
+        auto corr_products = [&](int kk) {
+          if constexpr (!kBF16) {
+            const uint64_t dh = ptx::smem_desc_sw128(bb + 32u * kk);
+            const uint64_t dl = ptx::smem_desc_sw128(bb + kBHalfT + 32u * kk);
+            mma_tf(d_corr, a_st + 8u * kk, dl, (s == 0 && kk == 0) ? 0u : 1u);
+            mma_tf(d_corr, a_st + 32u + 8u * kk, dh, 1u);
+          } else {
+            const uint32_t ak = a_st + 8u * kk;
+            mma_bf(d_corr, ak, bd(1, kk), (s == 0 && kk == 0) ? 0u : 1u);
+            mma_bf(d_corr, ak + 16u, bd(0, kk), 1u);
             if (kPieces == 3) {
-              ptx::mma_f16_ts(d_corr, ak + 16u, bd(1), kIdescP, 1u);
-              ptx::mma_f16_ts(d_corr, ak, bd(2), kIdescP, 1u);
-              ptx::mma_f16_ts(d_corr, ak + 32u, bd(0), kIdescP, 1u);
+              mma_bf(d_corr, ak + 16u, bd(1, kk), 1u);
+              mma_bf(d_corr, ak, bd(2, kk), 1u);
+              mma_bf(d_corr, ak + 32u, bd(0, kk), 1u);
             }
           }
+        };
+        auto main_product = [&](int kk) {
+          const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
+          if constexpr (!kBF16) mma_tf(d_main, a_st + 8u * kk, ptx::smem_desc_sw128(bb + 32u * kk), acc);
+          else mma_bf(d_main, a_st + 8u * kk, bd(0, kk), acc);
+        };
+        constexpr int kKK = kBF16 ? 2 : 4;
+#pragma unroll
+        for (int kk = 0; kk < kKK; ++kk) {
+          main_product(kk);
+          corr_products(kk);
         }
-        ptx::mma_commit(empty_bar(st));
-        if (kPanel) ptx::mma_commit(pempty(sb));
-        if ((s % kFold) == kFold - 1 || s == ksteps - 1) ptx::mma_commit(chunk_full(buf));
+        commit(empty_bar(st));
+        if (kPanel) commit(pempty(sb));
+        if ((s % kFold) == kFold - 1 || s == ksteps - 1) commit(chunk_full(buf));
       }
       // Signal the epilogue (also after an abort, so nobody waits forever),
       // then make sure no MMA is still writing TMEM before it is freed.
-      ptx::mma_commit(acc_bar);
+      commit(acc_bar);
       if (!ptx::mbar_wait(acc_bar, 0)) record_error(err_flag, kErrAccWait);
     }
     __syncwarp();
@@ -1384,9 +1450,9 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         if (AMode == kTmaKM)
           ptx::tma_load_2d(raw_a(r), &maps.a, static_cast<int>(kCx * k0), static_cast<int>(m0), raw_full(r));
         if (BMode == kTmaNK)
-          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(kCx * k0), static_cast<int>(n0), raw_full(r));
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(kCx * k0), static_cast<int>(nb0), raw_full(r));
         if (BMode == kTmaKN)
-          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(kCx * n0), static_cast<int>(k0), raw_full(r));
+          ptx::tma_load_2d(raw_b(r), &maps.b, static_cast<int>(kCx * nb0), static_cast<int>(k0), raw_full(r));
       }
       if (kGather) {
         if constexpr (kReal) {
@@ -1407,10 +1473,10 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           break;
         }
         const int x = static_cast<int>((kb / kStepKE + s) * kPanelBufs * 64);
-        ptx::mbar_arrive_expect_tx(pfull(sb), static_cast<uint32_t>(kPanelBufs * kBHalfBytes));
-        ptx::tma_load_2d(op0 + sb * kOpBytes, &maps.b, x, static_cast<int>(n0), pfull(sb));
+        ptx::mbar_arrive_expect_tx(pfull(sb), static_cast<uint32_t>(kPanelBufs * kBHalfT));
+        ptx::tma_load_2d(op0 + sb * kOpBytesT, &maps.b, x, static_cast<int>(n0), pfull(sb));
         if (kPanelBufs == 2)
-          ptx::tma_load_2d(op0 + sb * kOpBytes + kBHalfBytes, &maps.b, x + 64, static_cast<int>(n0),
+          ptx::tma_load_2d(op0 + sb * kOpBytesT + kBHalfT, &maps.b, x + 64, static_cast<int>(n0),
                            pfull(sb));
       }
     }
@@ -1460,15 +1526,16 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     const uint32_t areal = static_cast<uint32_t>(2 * kAK1 * wg * 512 + rho * 4);
     // TF32 B: piece j of this thread (id = pt + kConverters1 j) is two complex
     // k of one column ([n][k] tiles) or one k of two columns ([k][n] tile).
-    uint32_t bsrc[kBP1], boff[kBP1][2];
+    uint32_t bsrc[kBPT], boff[kBPT][2];
 #pragma unroll
-    for (int j = 0; j < kBP1; ++j) {
+    for (int j = 0; j < kBPT; ++j) {
       const int id = pt + kConverters1 * j;
       if (BMode == kTmaKN) {
-        // k: complex k, or (real) the k pair 2k, 2k + 1 (rows of 128 floats).
-        const int k = id >> 6, n = 2 * (id & 63);
+        // k: complex k, or (real) the k pair 2k, 2k + 1 (rows of kNCta
+        // complex or 128 real values).
+        const int k = id / (kNCta / 2), n = 2 * (id % (kNCta / 2));
         bsrc[j] = kReal ? static_cast<uint32_t>(2 * k * 512 + n * 4)
-                        : static_cast<uint32_t>(k * 1024 + n * 8);
+                        : static_cast<uint32_t>(k * kNCta * 8 + n * 8);
         boff[j][0] = swz128(n, k);
         boff[j][1] = swz128(n + 1, k);
       } else {
@@ -1484,19 +1551,19 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     // tile; one 16-byte chunk (8 bf16) per piece, chunk kq (+4 for odd
     // pieces) of row n.  Consecutive lanes take consecutive n: no bank
     // conflicts.
-    uint32_t b16src[kB16P1], b16row[kB16P1], b16chunk[kB16P1];
+    uint32_t b16src[kB16PT], b16row[kB16PT], b16chunk[kB16PT];
 #pragma unroll
-    for (int j = 0; j < kB16P1; ++j) {
+    for (int j = 0; j < kB16PT; ++j) {
       const int id = pt + kConverters1 * j;
-      const int n = id & 127, kq = id >> 7;
+      const int n = id % kNCta, kq = id / kNCta;
       b16src[j] = (BMode == kTmaKN)
                       ? (kReal ? static_cast<uint32_t>(8 * kq * 512 + n * 4)
-                               : static_cast<uint32_t>(4 * kq * 1024 + n * 8))
+                               : static_cast<uint32_t>(4 * kq * kNCta * 8 + n * 8))
                       : swz128(n, 4 * kq);
       b16row[j] = static_cast<uint32_t>((n >> 3) * 1024 + (n & 7) * 128);
       b16chunk[j] = static_cast<uint32_t>(kq ^ (n & 7));
     }
-    constexpr int kBV = kBP1 > 2 * kB16P1 ? kBP1 : 2 * kB16P1;
+    constexpr int kBV = kBPT > 2 * kB16PT ? kBPT : 2 * kB16PT;
 
     bool ok = true;
     int r = 0, st = 0;
@@ -1534,7 +1601,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       if constexpr (kPanel) {
       } else if constexpr (!kBF16) {
 #pragma unroll
-        for (int j = 0; j < kBP1; ++j) {
+        for (int j = 0; j < kBPT; ++j) {
           if (kReal && BMode == kTmaKN) {
             // Columns n, n + 1 of rows 2k, 2k + 1: pair (2k, 2k + 1) of each column.
             const float2 t0 = lds64(rb + bsrc[j]), t1 = lds64(rb + bsrc[j] + 512u);
@@ -1545,7 +1612,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         }
       } else {
 #pragma unroll
-        for (int j = 0; j < kB16P1; ++j) {
+        for (int j = 0; j < kB16PT; ++j) {
           if (kReal && BMode == kTmaKN) {
             // Column n, real k 8 kq .. 8 kq + 7 (rows of 128 floats).
             float v[8];
@@ -1554,8 +1621,9 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
             bv[2 * j] = make_float4(v[0], v[1], v[2], v[3]);
             bv[2 * j + 1] = make_float4(v[4], v[5], v[6], v[7]);
           } else if (BMode == kTmaKN) {
-            const float2 t0 = lds64(rb + b16src[j]), t1 = lds64(rb + b16src[j] + 1024u);
-            const float2 t2 = lds64(rb + b16src[j] + 2048u), t3 = lds64(rb + b16src[j] + 3072u);
+            constexpr uint32_t kRow = kNCta * 8;  // one k row of the raw [k][n] tile
+            const float2 t0 = lds64(rb + b16src[j]), t1 = lds64(rb + b16src[j] + kRow);
+            const float2 t2 = lds64(rb + b16src[j] + 2 * kRow), t3 = lds64(rb + b16src[j] + 3 * kRow);
             bv[2 * j] = make_float4(t0.x, t0.y, t1.x, t1.y);
             bv[2 * j + 1] = make_float4(t2.x, t2.y, t3.x, t3.y);
           } else {
@@ -1602,7 +1670,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         break;
       }
       ptx::tc_fence_after();
-      [[maybe_unused]] const uint32_t ob = op0 + st * kOpBytes;
+      [[maybe_unused]] const uint32_t ob = op0 + st * kOpBytesT;
       if constexpr (kBF16) {
         // A -> TMEM: kPieces bf16x2 words per pair, piece p at columns +16p.
         const uint32_t a_col = tmem + lane_base + kAStageCol + 64u * st + kAK1 * wg;
@@ -1610,7 +1678,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         for (int p = 0; p < kPieces; ++p) ptx::tmem_st_n<kAK1>(a_col + 16u * p, w[p]);
         // B -> shared memory: 4 complex k of column n, re/im interleaved.
 #pragma unroll
-        for (int j = 0; j < (kPanel ? 0 : kB16P1); ++j) {
+        for (int j = 0; j < (kPanel ? 0 : kB16PT); ++j) {
           float4 v0 = bv[2 * j], v1 = bv[2 * j + 1];
           if (conjB) {
             v0.y = -v0.y;
@@ -1625,7 +1693,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           split_bf16<kPieces>(v1.z, v1.w, qw[3][0], qw[3][1], qw[3][2]);
 #pragma unroll
           for (int p = 0; p < kPieces; ++p)
-            sts128(ob + (p >> 1) * kBHalfBytes + b16row[j] + ((b16chunk[j] ^ (4u * (p & 1))) << 4),
+            sts128(ob + (p >> 1) * kBHalfT + b16row[j] + ((b16chunk[j] ^ (4u * (p & 1))) << 4),
                    qw[0][p], qw[1][p], qw[2][p], qw[3][p]);
         }
       } else {
@@ -1635,7 +1703,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         ptx::tmem_st_n<2 * kAK1>(a_col + 32u, lo);
         // B -> shared memory (swizzled K-major hi and lo tiles).
 #pragma unroll
-        for (int j = 0; j < (kPanel ? 0 : kBP1); ++j) {
+        for (int j = 0; j < (kPanel ? 0 : kBPT); ++j) {
           float4 v = bv[j];
           if (conjB) {
             v.y = -v.y;
@@ -1646,11 +1714,11 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
           if (BMode == kTmaKN) {
             sts64(ob + boff[j][0], r0.hi, i0.hi);
             sts64(ob + boff[j][1], r1.hi, i1.hi);
-            sts64(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo);
-            sts64(ob + kBHalfBytes + boff[j][1], r1.lo, i1.lo);
+            sts64(ob + kBHalfT + boff[j][0], r0.lo, i0.lo);
+            sts64(ob + kBHalfT + boff[j][1], r1.lo, i1.lo);
           } else {
             sts128(ob + boff[j][0], r0.hi, i0.hi, r1.hi, i1.hi);
-            sts128(ob + kBHalfBytes + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
+            sts128(ob + kBHalfT + boff[j][0], r0.lo, i0.lo, r1.lo, i1.lo);
           }
         }
       }
@@ -1659,7 +1727,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       ptx::tc_fence_before();
       __syncwarp();
       if (lane == 0) {
-        ptx::mbar_arrive(full_bar(st));
+        arrive_mma(full_bar(st));
         ptx::mbar_arrive(raw_empty(r));
       }
 
@@ -1679,7 +1747,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         fold_from(buf ? kChunkCol1 : kChunkCol0);
         ptx::tc_fence_before();
         __syncwarp();
-        if (lane == 0) ptx::mbar_arrive(chunk_empty(buf));
+        if (lane == 0) arrive_mma(chunk_empty(buf));
       }
       if (++r == kRaw) {
         r = 0;
@@ -1717,11 +1785,14 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     }
   }
 
+  // A pair frees its TMEM together, once the MMAs (waited for by the even
+  // CTA's MMA thread) and every cross-CTA arrival are done.
   ptx::tc_fence_before();
-  __syncthreads();
+  if constexpr (kPair) ptx::cluster_sync(); else __syncthreads();
   if (warp == 0) {
     ptx::tc_fence_after();
-    ptx::tmem_dealloc(tmem, kTmemCols);
+    if constexpr (kPair) ptx::tmem_dealloc2(tmem, kTmemCols);
+    else ptx::tmem_dealloc(tmem, kTmemCols);
   }
 }
 
@@ -1779,21 +1850,66 @@ bool unit_blocks16(const std::vector<int64_t>& v, int64_t n) {
   return true;
 }
 
-template <int AMode, int BMode, int Prec, bool kReal>
+template <int AMode, int BMode, int Prec, bool kReal, bool kPair = false>
 cudaError_t launch_modes(const GemmArgs& args, const TmaMaps& maps, cudaStream_t stream,
                          int* err_flag, dim3 tiles) {
-  constexpr int kSmem = smem_bytes_1<kReal, BMode == kPanelNK>();
+  constexpr int kSmem = smem_bytes_1<kReal, BMode == kPanelNK, kPair>();
   static_assert(kSmem <= 227 * 1024, "shared memory budget");
   static bool attr_set = false;
   if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(tc1m_contract<AMode, BMode, Prec, kReal>,
+    cudaError_t e = cudaFuncSetAttribute(tc1m_contract<AMode, BMode, Prec, kReal, kPair>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
     if (e != cudaSuccess) return e;
     attr_set = true;
   }
-  tc1m_contract<AMode, BMode, Prec, kReal><<<tiles, kThreads1, kSmem, stream>>>(args, maps,
-                                                                                  err_flag);
-  return cudaGetLastError();
+  if constexpr (kPair) {
+    // Clusters of two CTAs along x (tiles.x counts CTAs: two per pair tile).
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = tiles;
+    cfg.blockDim = dim3(kThreads1);
+    cfg.dynamicSmemBytes = kSmem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, tc1m_contract<AMode, BMode, Prec, kReal, true>, args, maps,
+                              err_flag);
+  } else {
+    tc1m_contract<AMode, BMode, Prec, kReal, false><<<tiles, kThreads1, kSmem, stream>>>(
+        args, maps, err_flag);
+    return cudaGetLastError();
+  }
+}
+
+// CTA pairs: complex operands both loaded by TMA ([k][m] or [m][k] A,
+// [n][k] or [k][n] B); tiles.x = 2 x pair tiles.
+template <int Prec>
+cudaError_t launch_pair(int amode, int bmode, const GemmArgs& args, const TmaMaps& maps,
+                        cudaStream_t stream, int* err_flag, dim3 tiles) {
+  if (amode == kTmaMK) {
+    if (bmode == kTmaNK)
+      return launch_modes<kTmaMK, kTmaNK, Prec, false, true>(args, maps, stream, err_flag, tiles);
+    return launch_modes<kTmaMK, kTmaKN, Prec, false, true>(args, maps, stream, err_flag, tiles);
+  }
+  if (bmode == kTmaNK)
+    return launch_modes<kTmaKM, kTmaNK, Prec, false, true>(args, maps, stream, err_flag, tiles);
+  return launch_modes<kTmaKM, kTmaKN, Prec, false, true>(args, maps, stream, err_flag, tiles);
+}
+
+cudaError_t launch_pair_prec(int method, int amode, int bmode, const GemmArgs& args,
+                             const TmaMaps& maps, cudaStream_t stream, int* err_flag, dim3 tiles) {
+  switch (method) {
+    case T1M_METHOD_TC_BF16X3:
+      return launch_pair<kPrecBF16x3>(amode, bmode, args, maps, stream, err_flag, tiles);
+    case T1M_METHOD_TC_BF16X6:
+      return launch_pair<kPrecBF16x6>(amode, bmode, args, maps, stream, err_flag, tiles);
+    default:
+      return launch_pair<kPrecTF32x3>(amode, bmode, args, maps, stream, err_flag, tiles);
+  }
 }
 
 template <int AMode, int Prec, bool kReal>
@@ -2231,7 +2347,7 @@ size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel, size_t panel_bytes,
-                      void* pack, size_t pack_bytes, int* path) {
+                      void* pack, size_t pack_bytes, int* path, int form) {
   *kernels = 0;
   if (used_method) *used_method = method;
   if (path) *path = 0;
@@ -2424,11 +2540,31 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                    : (!a_block && p.amode == kAKM) ? kTmaKM : kGatherMK;
     int bm = (!b_block && p.bmode == kBNK) ? kTmaNK
              : (!b_block && p.bmode == kBKN) ? kTmaKN : kGatherNK;
-    if (panels)
-      if ((e = use_panels(p.g, &maps, &bm)) != cudaSuccess) return e;
-    e = launch_prec<false>(method, am, bm, p.g, maps, stream, err_flag, grid);
-    set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A,
-             packed_args.B != args.B);
+    // CTA pairs where both operands load by TMA and there are at least two
+    // 64-row M tiles: B is then split in-kernel, half per CTA, instead of by
+    // a panel pass.  Their B map takes 64-column boxes.
+    bool pair = form != T1M_TILE_ONE && am != kGatherMK && bm != kGatherNK && p.tiles_m >= 2;
+    TmaMaps pmaps;
+    if (pair) {
+      pmaps.a = p.map_a;
+      pair = bm == kTmaNK ? make_map(&pmaps.b, p.g.B, p.g.K, p.g.N, packed_plan->uB_n, 2 * kStepK,
+                                     kTileN / 2, true)
+                          : make_map(&pmaps.b, p.g.B, p.g.N, p.g.K, packed_plan->uB_k, kTileN,
+                                     kStepK, false);
+    }
+    if (pair) {
+      const int64_t pair_m = (p.g.M + 2 * kTileMc - 1) / (2 * kTileMc);
+      const dim3 pgrid(static_cast<unsigned>(2 * pair_m * p.tiles_n), static_cast<unsigned>(splits));
+      e = launch_pair_prec(method, am, bm, p.g, pmaps, stream, err_flag, pgrid);
+      set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A, false);
+      if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR;
+    } else {
+      if (panels)
+        if ((e = use_panels(p.g, &maps, &bm)) != cudaSuccess) return e;
+      e = launch_prec<false>(method, am, bm, p.g, maps, stream, err_flag, grid);
+      set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A,
+               packed_args.B != args.B);
+    }
   } else {
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
     set_path(p.amode, p.bmode, true, packed_args.A != args.A, packed_args.B != args.B);

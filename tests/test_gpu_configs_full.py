@@ -203,15 +203,22 @@ def _config3_check(ctx, torch, ga, gb, methods, tol, samples=512):
 @pytest.mark.slow
 @pytest.mark.parametrize("inputs", ["uniform", "logmag"])
 def test_config3_3xtf32_full_size(ctx, torch_cuda, inputs):
-    """complex64 ijkl,klmn->ijmn at 4096^3, both input sets: 3xTF32 (B panels)
-    and the automatic method (BF16x6) within 1e-6 of sampled FP64."""
+    """complex64 ijkl,klmn->ijmn at 4096^3, both input sets: 3xTF32 and the
+    automatic method (BF16x6), on CTA pairs (the automatic tile form) and on
+    one tile per CTA (3xTF32 with B panels), within 1e-6 of sampled FP64."""
     import t1m_gb300 as t1m
     torch = torch_cuda
     ga, gb = _config3_inputs(torch, inputs, torch.complex64)
     reps = _config3_check(ctx, torch, ga, gb, ["tc_3xtf32", "auto"], TOL)
     assert reps["tc_3xtf32"].method == t1m.method.tc_3xtf32
-    assert reps["tc_3xtf32"].fetch["b"] == "panels"
+    assert reps["tc_3xtf32"].fetch["pair"] and reps["auto"].fetch["pair"]
     assert reps["auto"].method == t1m.method.tc_bf16x6
+    ctx.set_tile_form("one")
+    try:
+        reps = _config3_check(ctx, torch, ga, gb, ["tc_3xtf32"], TOL)
+    finally:
+        ctx.set_tile_form("auto")
+    assert reps["tc_3xtf32"].fetch["b"] == "panels" and not reps["tc_3xtf32"].fetch["pair"]
 
 
 @pytest.mark.slow

@@ -10,6 +10,15 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
+
+@pytest.fixture(autouse=True)
+def _one_tile_form(ctx):
+    """Panels feed the one-tile-per-CTA kernel; where both operands load by
+    TMA the automatic form runs CTA pairs instead (B split in-kernel)."""
+    ctx.set_tile_form("one")
+    yield
+    ctx.set_tile_form("auto")
+
 TOL = {"tc_3xtf32": 1e-6, "tc_bf16x6": 1e-6, "tc_bf16x3": 2e-5}
 
 
