@@ -197,8 +197,9 @@ def sampled_entries(flat_a, flat_b, scat, rows, cols):
 
 def rel_errors(got, ref):
     """(normwise max, Frobenius) relative error of ``got`` against ``ref``."""
-    got = np.asarray(got).astype(np.complex128 if np.iscomplexobj(ref) else np.float64)
     ref = np.asarray(ref)
+    cplx = np.iscomplexobj(ref) or np.iscomplexobj(got)
+    got = np.asarray(got).astype(np.complex128 if cplx else np.float64)
     d = np.abs(got - ref)
     mx = float(d.max() / max(np.abs(ref).max(), np.finfo(np.float64).tiny))
     fro = float(np.linalg.norm(d.reshape(-1)) /

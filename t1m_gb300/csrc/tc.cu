@@ -1194,6 +1194,19 @@ static_assert(kAK1 % 4 == 0 && kMC1 % 32 == 0 && kBP1 >= 1 && kB16P1 >= 1, "conv
 // 4-stage A ring with a single chunk accumulator measured slower in both
 // (the MMA thread then waits for each fold before a chunk's main products).
 constexpr int kBarrierBytes1 = 256;
+// MMA issue by two threads (different warps) for 3xTF32: one issues the main
+// products into the chunk accumulators, the other the correction products
+// into their accumulator.  Each accumulator still sees one thread's products
+// in a fixed order (results unchanged, bit for bit).  Measured at complex64
+// 4096^3 (pairs): 3xTF32 200 -> 208 TFLOP/s; BF16x6 218 -> 202 and BF16x3
+// 293 -> 286, so the bf16 forms keep one issuer.  A thread issuing MMAs
+// stalls while the tensor pipe's queue is full, so the split helps only
+// where its own issue work is the longer part.  Needs a free warp: loaders
+// that gather use all three loader warps.
+template <int Prec>
+constexpr bool split_mma_issue() {
+  return Prec == kPrecTF32x3;
+}
 template <bool kReal, bool kPanel, bool kPair = false>
 constexpr int smem_bytes_1() {
   return 1024 +
@@ -1283,10 +1296,12 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     }
   }
   if (tid == 32) {
+    // Barriers the MMA issuers commit to count one commit per issuer.
+    constexpr uint32_t kIssuers = (split_mma_issue<Prec>() && !kGather) ? 2u : 1u;
     if (kPanel) {
       for (int i = 0; i < kPanelStages; ++i) {
         ptx::mbar_init(pfull(i), 1);
-        ptx::mbar_init(pempty(i), 1);
+        ptx::mbar_init(pempty(i), kIssuers);
       }
     }
     for (int r = 0; r < kRaw; ++r) {
@@ -1295,13 +1310,13 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     }
     for (int s = 0; s < kStages; ++s) {
       ptx::mbar_init(full_bar(s), kConvArrivals);
-      ptx::mbar_init(empty_bar(s), 1);
+      ptx::mbar_init(empty_bar(s), kIssuers);
     }
     for (int b = 0; b < 2; ++b) {
       ptx::mbar_init(chunk_full(b), 1);
       ptx::mbar_init(chunk_empty(b), kConvArrivals);
     }
-    ptx::mbar_init(acc_bar, 1);
+    ptx::mbar_init(acc_bar, kIssuers);
     ptx::fence_mbar_init();
   }
   if (tid == 64) {
@@ -1355,16 +1370,26 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   const int64_t nb0 = n0 + rank * kNCta;  // first B column this CTA loads
   const int64_t ksteps = (K - kb + kStepKE - 1) / kStepKE;
 
-  if (warp == 0) {
+  // Threads issuing MMAs: lane 0 of warp 0 (main products, or all), and with
+  // a split issue lane 0 of warp 3 (correction products).
+  constexpr bool kSplitIssue = split_mma_issue<Prec>() && !kGather;
+  if (warp == 0 || (kSplitIssue && warp == 3)) {
     // ---------------------------------------------------------- MMA issue ---
+    const bool issue_main = warp == 0;
+    const bool issue_corr = !kSplitIssue || warp == 3;
     if (lane == 0 && rank == 0) {
+      // Descriptors: the 14-bit start-address field of a shared-memory
+      // descriptor is address >> 4, so a descriptor at a byte offset is the
+      // base descriptor plus offset >> 4.
+      const uint64_t desc0 = ptx::smem_desc_sw128(op0);
+      const uint32_t d_corr = tmem + kCorrCol;
       for (int64_t s = 0; s < ksteps; ++s) {
         const int st = static_cast<int>(s % kStages);
         const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
         const int64_t c = s / kFold;
         const int buf = static_cast<int>(c & 1);
         const bool chunk_start = (s % kFold) == 0;
-        if (chunk_start && c >= 2 &&
+        if (issue_main && chunk_start && c >= 2 &&
             !wait_conv(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
           record_error(err_flag, kErrChunkWait);
           break;
@@ -1380,48 +1405,49 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         }
         ptx::tc_fence_after();
         const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
-        const uint32_t d_corr = tmem + kCorrCol;
         const uint32_t a_st = tmem + kAStageCol + 64u * st;
-        const uint32_t bb = op0 + sb * kOpBytesT;
+        const uint64_t db = desc0 + static_cast<uint64_t>((sb * kOpBytesT) >> 4);
         // One stage: TF32x3 (kind::tf32, K = 8): 4 x (hi.hi -> main, hi.lo +
         // lo.hi -> corrections).  bf16 (kind::f16, K = 16): A piece p at 16
         // TMEM columns +16p, B piece p in 64-byte half (p & 1) of B buffer
         // (p >> 1); 2 x (x0y0 -> main, x0y1 + x1y0 [+ x1y1 + x0y2 + x2y0] ->
         // corrections).
         auto bd = [&](int p, int kk) {
-          return ptx::smem_desc_sw128(bb + (p >> 1) * kBHalfT + 64u * (p & 1) + 32u * kk);
-        };
-        auto corr_products = [&](int kk) {
-          if constexpr (!kBF16) {
-            const uint64_t dh = ptx::smem_desc_sw128(bb + 32u * kk);
-            const uint64_t dl = ptx::smem_desc_sw128(bb + kBHalfT + 32u * kk);
-            mma_tf(d_corr, a_st + 8u * kk, dl, (s == 0 && kk == 0) ? 0u : 1u);
-            mma_tf(d_corr, a_st + 32u + 8u * kk, dh, 1u);
-          } else {
-            const uint32_t ak = a_st + 8u * kk;
-            mma_bf(d_corr, ak, bd(1, kk), (s == 0 && kk == 0) ? 0u : 1u);
-            mma_bf(d_corr, ak + 16u, bd(0, kk), 1u);
-            if (kPieces == 3) {
-              mma_bf(d_corr, ak + 16u, bd(1, kk), 1u);
-              mma_bf(d_corr, ak, bd(2, kk), 1u);
-              mma_bf(d_corr, ak + 32u, bd(0, kk), 1u);
-            }
-          }
-        };
-        auto main_product = [&](int kk) {
-          const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
-          if constexpr (!kBF16) mma_tf(d_main, a_st + 8u * kk, ptx::smem_desc_sw128(bb + 32u * kk), acc);
-          else mma_bf(d_main, a_st + 8u * kk, bd(0, kk), acc);
+          return db + static_cast<uint64_t>(((p >> 1) * kBHalfT + 64 * (p & 1) + 32 * kk) >> 4);
         };
         constexpr int kKK = kBF16 ? 2 : 4;
+        if (issue_main) {
 #pragma unroll
-        for (int kk = 0; kk < kKK; ++kk) {
-          main_product(kk);
-          corr_products(kk);
+          for (int kk = 0; kk < kKK; ++kk) {
+            const uint32_t acc = (chunk_start && kk == 0) ? 0u : 1u;
+            if constexpr (!kBF16) mma_tf(d_main, a_st + 8u * kk, db + 2u * kk, acc);
+            else mma_bf(d_main, a_st + 8u * kk, bd(0, kk), acc);
+          }
+        }
+        if (issue_corr) {
+#pragma unroll
+          for (int kk = 0; kk < kKK; ++kk) {
+            const uint32_t first = (s == 0 && kk == 0) ? 0u : 1u;
+            if constexpr (!kBF16) {
+              const uint64_t dh = db + 2u * kk;
+              const uint64_t dl = db + static_cast<uint64_t>((kBHalfT + 32 * kk) >> 4);
+              mma_tf(d_corr, a_st + 8u * kk, dl, first);
+              mma_tf(d_corr, a_st + 32u + 8u * kk, dh, 1u);
+            } else {
+              const uint32_t ak = a_st + 8u * kk;
+              mma_bf(d_corr, ak, bd(1, kk), first);
+              mma_bf(d_corr, ak + 16u, bd(0, kk), 1u);
+              if (kPieces == 3) {
+                mma_bf(d_corr, ak + 16u, bd(1, kk), 1u);
+                mma_bf(d_corr, ak, bd(2, kk), 1u);
+                mma_bf(d_corr, ak + 32u, bd(0, kk), 1u);
+              }
+            }
+          }
         }
         commit(empty_bar(st));
         if (kPanel) commit(pempty(sb));
-        if ((s % kFold) == kFold - 1 || s == ksteps - 1) commit(chunk_full(buf));
+        if (issue_main && ((s % kFold) == kFold - 1 || s == ksteps - 1)) commit(chunk_full(buf));
       }
       // Signal the epilogue (also after an abort, so nobody waits forever),
       // then make sure no MMA is still writing TMEM before it is freed.
