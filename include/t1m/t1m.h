@@ -113,6 +113,8 @@ class context {
   void set_workspace_limit(int64_t bytes) { check(t1m_set_workspace_limit(h_, bytes)); }
   /// Tile form of tensor-core products (T1M_TILE_AUTO / _ONE / _PAIR).
   void set_tile_form(int form) { check(t1m_set_tile_form(h_, form)); }
+  /// Bound on grouped launches' dependency waits in microseconds (0 = default).
+  void set_wait_limit(int64_t us) { check(t1m_set_wait_limit(h_, us)); }
   /// Run on a caller-owned cudaStream_t (nullptr = the context's own stream).
   void set_stream(void* stream) { check(t1m_set_stream(h_, stream)); }
   void synchronize() { check(t1m_synchronize(h_)); }

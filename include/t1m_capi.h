@@ -148,6 +148,11 @@ int t1m_set_split_k(t1m_context* ctx, int splits);
  * No reference counterpart (the reference packs into one aligned_alloc'ed
  * buffer per call, t1m.h:450-460). */
 int t1m_set_workspace_limit(t1m_context* ctx, int64_t bytes);
+/* Bound, in microseconds, on the device-side waits of grouped launches for
+ * the items they depend on (0, the default: about two seconds).  Applies to
+ * groups created afterwards.  A wait that runs out sets the error word, and
+ * the call that synchronises next returns T1M_ERR_KERNEL_TIMEOUT. */
+int t1m_set_wait_limit(t1m_context* ctx, int64_t microseconds);
 /* Tile form of single tensor-core contractions (complex64).  T1M_TILE_PAIR
  * runs clusters of two CTAs whose MMAs (tcgen05 cta_group::2, 256 x 128 real
  * tiles) each read half of B from either CTA, where both operands load by
@@ -222,6 +227,14 @@ typedef struct t1m_group t1m_group;
 
 #define T1M_GROUP_GRAPH 1u
 #define T1M_GROUP_AUTOTUNE 2u
+/* Failure injection for tests of the timeout path (host side; no fault on
+ * the GPU): every dependent item of a single persistent launch waits for one
+ * more tile than its dependency writes, a count nothing reaches.  Its bounded
+ * waits run out (t1m_set_wait_limit), its remaining stages are drained
+ * without loads, the launch completes, and t1m_group_launch reports
+ * T1M_ERR_KERNEL_TIMEOUT; the context stays usable.  Outputs of such a
+ * launch are undefined. */
+#define T1M_GROUP_INJECT_UNMET_DEPENDENCY 4u
 
 int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_group_item* items,
                      uint32_t options, t1m_group** group);

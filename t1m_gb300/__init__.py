@@ -125,6 +125,7 @@ class GroupItem(C.Structure):
 
 GROUP_GRAPH = 1
 GROUP_AUTOTUNE = 2
+GROUP_INJECT_UNMET_DEPENDENCY = 4
 
 _lib_handle: C.CDLL | None = None
 
@@ -146,6 +147,7 @@ def lib() -> C.CDLL:
         h.t1m_set_split_k.argtypes = [vp, i32]
         h.t1m_set_workspace_limit.argtypes = [vp, C.c_int64]
         h.t1m_set_tile_form.argtypes = [vp, i32]
+        h.t1m_set_wait_limit.argtypes = [vp, C.c_int64]
         h.t1m_synchronize.argtypes = [vp]
         h.t1m_status_string.restype = C.c_char_p
         h.t1m_status_string.argtypes = [i32]
@@ -198,6 +200,11 @@ class Context:
         if isinstance(form, str):
             form = TILE_FORMS[form]
         self._check(lib().t1m_set_tile_form(self._h, int(form)))
+
+    def set_wait_limit(self, microseconds: int) -> None:
+        """Bound on grouped launches' device-side dependency waits (us; 0 =
+        the default of about two seconds), for groups created afterwards."""
+        self._check(lib().t1m_set_wait_limit(self._h, int(microseconds)))
 
     def set_stream(self, stream: int | None) -> None:
         self._check(lib().t1m_set_stream(self._h, stream or None))
@@ -394,7 +401,7 @@ class Group:
     earlier item whose C this one reads, or -1)."""
 
     def __init__(self, items, ctx: Context | None = None, graph: bool = True,
-                 autotune: bool = False):
+                 autotune: bool = False, options: int = 0):
         self.ctx = ctx or default_context()
         self._h = C.c_void_p()
         self._keep: list = []
@@ -412,7 +419,7 @@ class Group:
             raise TypeError(f"mixed element types {dtypes}")
         dtype = _DTYPE_OF[dtypes.pop()] if dtypes else COMPLEX64
         self._keep.append(arr)
-        opts = (GROUP_GRAPH if graph else 0) | (GROUP_AUTOTUNE if autotune else 0)
+        opts = (GROUP_GRAPH if graph else 0) | (GROUP_AUTOTUNE if autotune else 0) | options
         st = lib().t1m_group_create(self.ctx.handle, dtype, len(items), arr, opts,
                                     C.byref(self._h))
         if st != OK:

@@ -67,6 +67,10 @@ struct t1m_context {
   int64_t opt_work_limit = -1;
   // T1M_TILE_* form of tensor-core products.
   int tile_form = T1M_TILE_AUTO;
+  // Bound on grouped launches' dependency waits (us, 0 = kernel default) and
+  // the SM clock (kHz) that converts it to clock64 cycles.
+  int64_t wait_limit_us = 0;
+  int clock_khz = 2070000;
   // T1M_PATH_* code of the last tensor-core product of the current call.
   int last_path = 0;
   int num_sms = 152;
@@ -700,7 +704,16 @@ int t1m_create(t1m_context** out, int device) {
   }
   ctx->stream = ctx->own_stream;
   ctx->num_sms = prop.multiProcessorCount;
+  int khz = 0;
+  if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device) == cudaSuccess && khz > 0)
+    ctx->clock_khz = khz;
   *out = ctx;
+  return T1M_OK;
+}
+
+int t1m_set_wait_limit(t1m_context* ctx, int64_t microseconds) {
+  if (!ctx || microseconds < 0) return T1M_ERR_INVALID_ARGUMENT;
+  ctx->wait_limit_us = microseconds;
   return T1M_OK;
 }
 
@@ -1549,10 +1562,13 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
           tp.tile_begin = (all_tc ? g->tc_total : L.tiles);
           tp.dep = -1;
           tp.dep_tiles = 0;
+          tp.dep_wait_cycles = ctx->wait_limit_us * (ctx->clock_khz / 1000);
           if (all_tc && items[i].depends_on >= 0) {
             const TcProblem& d = tcs[tc_index[items[i].depends_on]];
             tp.dep = tc_index[items[i].depends_on];
             tp.dep_tiles = static_cast<int32_t>(tc_problem_tiles(d));
+            // Test aid: a count the dependency never reaches.
+            if (options & T1M_GROUP_INJECT_UNMET_DEPENDENCY) ++tp.dep_tiles;
           }
           tc_index[i] = static_cast<int>(tcs.size());
           const int64_t t = tc_problem_tiles(tp);

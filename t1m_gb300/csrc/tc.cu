@@ -680,6 +680,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
     // ------------------------------------------------------------ loaders ---
     const int lt = tid - kLoaderBase;  // 0..95
     int64_t raw_cnt = 0;
+    bool dep_failed = false;  // a dependency wait of this thread ran out
     for (int64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
       const TileRef tr = locate(&single, group, nprob, t);
       const TcProblem* p = tr.p;
@@ -712,24 +713,32 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         continue;
       }
       bool stop = false;
-      if (done && p->dep >= 0) {
+      if (done && p->dep >= 0 && !dep_failed) {
         // This problem reads the C of problem p->dep: wait (bounded) until all
         // of its tiles are written, then order those generic-proxy writes
         // before this thread's TMA / cp.async reads.
         const int* ctr = done + p->dep;
+        const long long budget = p->dep_wait_cycles > 0 ? p->dep_wait_cycles : ptx::kSpinBudget;
         if (ld_acquire(ctr) < p->dep_tiles) {
           const long long t0 = clock64();
           while (ld_acquire(ctr) < p->dep_tiles) {
             __nanosleep(200);
-            if (clock64() - t0 > ptx::kSpinBudget) {
+            if (clock64() - t0 > budget) {
               record_error(err_flag, kErrDepWait);
-              stop = true;
+              dep_failed = true;
               break;
             }
           }
         }
         asm volatile("fence.proxy.async.global;" ::: "memory");
       }
+      // After a dependency wait ran out, this thread's remaining stages of
+      // dependent problems are drained rather than loaded: it still arrives
+      // on every raw stage it owes, so the converters and the MMA thread run
+      // their pipelines to the end (no wait of theirs runs out, every MMA
+      // completes before TMEM is freed); the outputs of such a launch are
+      // undefined, and the error word reports it.
+      const bool drain = dep_failed && p->dep >= 0;
       for (int64_t s = 0; s < tr.ksteps && !stop; ++s, ++raw_cnt) {
         const int r = static_cast<int>(raw_cnt % kRaw);
         const uint32_t ph = static_cast<uint32_t>((raw_cnt / kRaw) & 1);
@@ -738,6 +747,13 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           record_error(err_flag, kErrRawWait);
           stop = true;
           break;
+        }
+        if (drain) {
+          // The arrivals a loaded stage would bring: the TMA thread's one
+          // (plus the skipped loaders' on TMA-only tiles), one per gatherer.
+          if (lt == 0) ptx::mbar_arrive_count(raw_full(r), gathering ? 1u : 1u + kLoaders);
+          if (gathering) ptx::mbar_arrive(raw_full(r));
+          continue;
         }
         if (lt == 0) {
           const uint32_t bytes = (amode != kAGather ? kRawABytes : 0) +

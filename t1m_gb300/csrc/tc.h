@@ -47,6 +47,9 @@ struct TcProblem {
   // scatter vector); bit 1: the same for B.
   int32_t block_maps;
   int64_t tile_begin;  // first tile of this problem in the launch's tile list
+  // Bound, in SM clock cycles, on the wait for the dependency's tiles (0:
+  // the kernels' default of about two seconds).
+  int64_t dep_wait_cycles;
 };
 
 // Fill a descriptor (fetch modes, tensor maps, tile counts).  False if the
