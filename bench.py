@@ -59,8 +59,11 @@ def _peaks() -> dict:
             "sm_max_mhz": 2070.0, "_source": "fallback"}
 
 
+# ncu summaries of the dominant kernel per method (CTA-pair form for BF16x6,
+# the automatic tile form of this workload; the 3xTF32 summary is of the
+# one-CTA form with B panels).
 PROFILE_OF = {"tc_3xtf32": "tc1m_contract_ijkl_klmn_64.md",
-              "tc_bf16x6": "tc1m_contract_bf16x6_ijkl_klmn_64.md"}
+              "tc_bf16x6": "tc1m_contract_pair_bf16x6_ijkl_klmn_64.md"}
 
 
 def _profiled_traffic(method):
