@@ -676,13 +676,18 @@ def workload_vjp(args):
     chain = ContractionChain(labels, outs)
     one = torch.ones((), dtype=torch.complex64, device=dev)
     chain_ms = _events_ms(torch, lambda: chain.backward(xs, one, ctx=ctx), 5, 2)
+    # The same chain as one grouped launch per pass (forward + adjoint).
+    gchain = ContractionChain(labels, outs, mode="grouped")
+    gchain_ms = _events_ms(torch, lambda: gchain.backward(xs, one, ctx=ctx), 5, 2)
+    gchain.close()
     ctx.close()
     print(json.dumps({"workload": "config5 abcd,ebfd->aecf extents 32 + VJP; ring chain",
                       "forward_ms": fwd_ms, "forward_tflops": flops / fwd_ms / 1e9,
                       "vjp_ms": vjp_ms, "vjp_tflops": 2 * flops / vjp_ms / 1e9,
                       "vjp_kernel_ms_reported": vrep.kernel_ms, "vjp_kernels": vrep.kernels,
                       "rel_err_dA": eA, "rel_err_dB": eB,
-                      "ring_chain_backward_ms": chain_ms}), flush=True)
+                      "ring_chain_backward_ms": chain_ms,
+                      "ring_chain_backward_grouped_ms": gchain_ms}), flush=True)
 
 
 def main() -> None:

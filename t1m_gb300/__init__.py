@@ -396,9 +396,10 @@ def contract_vjp(dc: tensor, lc: str, a: tensor, la: str, b: tensor, lb: str,
 class Group:
     """A batch of contractions run as grouped launches (t1m_group_*).
 
-    ``items``: sequence of (alpha, a, la, b, lb, beta, c, lc, depends_on)
-    with device tensors (C = alpha*A*B + beta*C; depends_on = index of an
-    earlier item whose C this one reads, or -1)."""
+    ``items``: sequence of (alpha, a, la, b, lb, beta, c, lc, depends_on
+    [, flags]) with device tensors (C = alpha*A*B + beta*C; depends_on =
+    index of an earlier item whose C this one reads, or -1; flags: FLAG_CONJ_A
+    / FLAG_CONJ_B / FLAG_ACCUMULATE, default 0)."""
 
     def __init__(self, items, ctx: Context | None = None, graph: bool = True,
                  autotune: bool = False, options: int = 0):
@@ -407,14 +408,16 @@ class Group:
         self._keep: list = []
         arr = (GroupItem * max(1, len(items)))()
         dtypes = set()
-        for i, (alpha, a, la, b, lb, beta, c, lc, dep) in enumerate(items):
+        for i, item in enumerate(items):
+            alpha, a, la, b, lb, beta, c, lc, dep = item[:9]
+            flags = int(item[9]) if len(item) > 9 else 0
             dtypes |= {a.dtype(), b.dtype(), c.dtype()}
             ta, tb, tc = a._c(self._keep), b._c(self._keep), c._c(self._keep)
             self._keep += [ta, tb, tc]
             al, be = complex(alpha), complex(beta)
             arr[i] = GroupItem(C.pointer(ta), la.encode(), C.pointer(tb), lb.encode(),
                                C.pointer(tc), lc.encode(), (C.c_double * 2)(al.real, al.imag),
-                               (C.c_double * 2)(be.real, be.imag), int(dep), 0)
+                               (C.c_double * 2)(be.real, be.imag), int(dep), flags)
         if len(dtypes) > 1:
             raise TypeError(f"mixed element types {dtypes}")
         dtype = _DTYPE_OF[dtypes.pop()] if dtypes else COMPLEX64

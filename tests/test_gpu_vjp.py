@@ -175,3 +175,42 @@ def test_ring_chain_complex64_tensor_cores_vs_complex128(ctx, torch_cuda):
     for a, b in zip(g64, g128):
         err = (a.to(torch.complex128) - b).abs().max().item() / b.abs().max().item()
         assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("dt,bond,phys", [("complex128", 8, 2), ("complex128", 64, 8),
+                                          ("complex64", 64, 8)])
+def test_ring_chain_grouped_mode(ctx, torch_cuda, dt, bond, phys):
+    """The chain as one grouped launch per pass (intermediates kept in device
+    memory, adjoint products as conjugating group items): forward value and
+    gradients equal the recomputing chain's and torch autograd's, and replays
+    of the planned groups give the same results."""
+    from t1m_gb300.chain import ContractionChain
+    torch = torch_cuda
+    rng = np.random.default_rng(13)
+    labels, outs = RING
+    ext = dict(a=bond, b=bond, c=bond, d=bond, p=phys, q=phys)
+    scale = 1.0 / np.sqrt(bond)
+    xs = [_dev(torch, scale * _rand(rng, [ext[c] for c in lab], np.complex128)).to(
+        getattr(torch, dt)) for lab in labels]
+    one = torch.ones((), dtype=xs[0].dtype, device="cuda")
+    ref_chain = ContractionChain(labels, outs)
+    s_ref = complex(ref_chain.forward(xs, ctx=ctx).cpu())
+    g_ref = ref_chain.backward(xs, one, ctx=ctx)
+    chain = ContractionChain(labels, outs, mode="grouped")
+    tol = 1e-10 if dt == "complex128" else 2e-5
+    try:
+        for _ in range(2):  # first call plans the groups, the second replays them
+            s = complex(chain.forward(xs, ctx=ctx).cpu())
+            grads = [g.clone() for g in chain.backward(xs, one, ctx=ctx)]
+            assert abs(s - s_ref) <= tol * max(1.0, abs(s_ref)), (s, s_ref)
+            for g, r in zip(grads, g_ref):
+                err = (g.to(torch.complex128) - r.to(torch.complex128)).abs().max().item()
+                assert err <= tol * max(1.0, r.abs().max().item()), err
+    finally:
+        chain.close()
+    # torch autograd of einsum in complex128 as an independent check.
+    ts = [x.to(torch.complex128).clone().requires_grad_(True) for x in xs]
+    torch.einsum("apb,bpc,cqd,dqa->", *ts).real.backward()
+    for g, t in zip(grads, ts):
+        err = (g.to(torch.complex128) - t.grad).abs().max().item()
+        assert err <= max(tol, 1e-5 if dt == "complex64" else 1e-10) * max(1.0, t.grad.abs().max().item())
