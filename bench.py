@@ -248,6 +248,7 @@ def run_gpu(args) -> None:
 
     ctx = t1m.Context(local)
     ctx.set_tile_form(args.tile_form)
+    ctx.set_autotune(args.autotune)
     dev = torch.device("cuda", local)
     g = torch.Generator(device=dev)
     g.manual_seed(1234 + rank)
@@ -378,6 +379,7 @@ def run_gpu(args) -> None:
             "scaling": "weak", "vs_baseline": None, "dtype": "complex64",
             "data": "synthetic (re/im U[-1,1], torch seed 1234+rank)",
             "config": {"workload": WORKLOAD, "method": tc_method, "tile_form": args.tile_form,
+                       "autotune": bool(args.autotune), "split_k": rep0.split_k,
                        "tile_path": rep0.fetch,
                        "l2": "inputs larger than L2 (A, B, C 134 MB each)",
                        "parallelism": f"replicas x{world}"},
@@ -699,6 +701,8 @@ def main() -> None:
     ap.add_argument("--method", default="auto")
     ap.add_argument("--tile-form", default="auto", choices=["auto", "one", "pair"],
                     help="tensor-core tile form (one tile per CTA or CTA pairs)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="tune tile form and split count per shape class (first call)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="headline",
                     choices=["headline", "config2", "logmag", "c128", "batch", "vjp"])

@@ -115,6 +115,8 @@ class context {
   void set_tile_form(int form) { check(t1m_set_tile_form(h_, form)); }
   /// Bound on grouped launches' dependency waits in microseconds (0 = default).
   void set_wait_limit(int64_t us) { check(t1m_set_wait_limit(h_, us)); }
+  /// Tune single tensor-core contractions per shape class (cached).
+  void set_autotune(bool on) { check(t1m_set_autotune(h_, on ? 1 : 0)); }
   /// Run on a caller-owned cudaStream_t (nullptr = the context's own stream).
   void set_stream(void* stream) { check(t1m_set_stream(h_, stream)); }
   void synchronize() { check(t1m_synchronize(h_)); }

@@ -163,6 +163,16 @@ int t1m_set_wait_limit(t1m_context* ctx, int64_t microseconds);
 #define T1M_TILE_ONE 1
 #define T1M_TILE_PAIR 2
 int t1m_set_tile_form(t1m_context* ctx, int form);
+/* Autotuning of single tensor-core contractions (on != 0; default off): per
+ * shape class (element type, method, log2 of M, N and K, which operand
+ * directions have unit stride) the tile form (one CTA or CTA pairs) and the
+ * split-K count (the heuristic count, half or twice it, never below the
+ * automatic method's precision minimum) are measured once on the call's own
+ * operands, into scratch outputs, and the fastest is cached in the same file
+ * as the grouped launches' choices ($T1M_TUNE_CACHE).  Applies when the tile
+ * form and the split count are automatic.  The reference's counterpart is
+ * BLIS's fixed block sizes (bli/mappings.h:101-142). */
+int t1m_set_autotune(t1m_context* ctx, int on);
 int t1m_synchronize(t1m_context* ctx);
 const char* t1m_status_string(int status);
 const char* t1m_last_error(const t1m_context* ctx);

@@ -148,6 +148,7 @@ def lib() -> C.CDLL:
         h.t1m_set_workspace_limit.argtypes = [vp, C.c_int64]
         h.t1m_set_tile_form.argtypes = [vp, i32]
         h.t1m_set_wait_limit.argtypes = [vp, C.c_int64]
+        h.t1m_set_autotune.argtypes = [vp, i32]
         h.t1m_synchronize.argtypes = [vp]
         h.t1m_status_string.restype = C.c_char_p
         h.t1m_status_string.argtypes = [i32]
@@ -200,6 +201,11 @@ class Context:
         if isinstance(form, str):
             form = TILE_FORMS[form]
         self._check(lib().t1m_set_tile_form(self._h, int(form)))
+
+    def set_autotune(self, on: bool) -> None:
+        """Tune single tensor-core contractions (tile form, split count) once
+        per shape class; choices cached in $T1M_TUNE_CACHE."""
+        self._check(lib().t1m_set_autotune(self._h, int(bool(on))))
 
     def set_wait_limit(self, microseconds: int) -> None:
         """Bound on grouped launches' device-side dependency waits (us; 0 =

@@ -71,6 +71,9 @@ struct t1m_context {
   // the SM clock (kHz) that converts it to clock64 cycles.
   int64_t wait_limit_us = 0;
   int clock_khz = 2070000;
+  // Tune single tensor-core contractions (tile form, split count) per shape
+  // class, cached with the grouped launches' choices.
+  bool autotune = false;
   // T1M_PATH_* code of the last tensor-core product of the current call.
   int last_path = 0;
   int num_sms = 152;
@@ -307,6 +310,12 @@ bool ensure_opt_work(cudaStream_t user, void** buf, size_t* have, size_t bytes) 
   return true;
 }
 
+// Tuned tile form and split count of a single tensor-core product (defined
+// with the tuning cache below); false when none applies.
+bool tuned_product(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
+                   const GemmArgs& g, cudaStream_t s, int slot, int* form, int* splits,
+                   int64_t* k_per_split);
+
 // One product C = alpha*A*B (+ beta*C) on stream s, its operands already in
 // g (shifted for a batch index or a slab): method checks, split-K (raw
 // partials in the workspace, FP64 reduction with the epilogue) and the
@@ -336,6 +345,17 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
     splits = allow_split ? choose_splits(ctx, method, dtype, g.M, g.N, g.K, es, &kps,
                                          ctx->method == T1M_METHOD_AUTO)
                          : 1;
+    int form = ctx->tile_form;
+    if (allow_split && ctx->autotune && ctx->split_k == 0 && ctx->tile_form == T1M_TILE_AUTO &&
+        method != T1M_METHOD_PLAIN && method != T1M_METHOD_DMMA) {
+      int tf = 0, ts = 0;
+      int64_t tk = 0;
+      if (tuned_product(ctx, method, dtype, es, hp, g, s, slot, &tf, &ts, &tk)) {
+        form = tf;
+        splits = ts;
+        kps = tk;
+      }
+    }
     // Split-K: the main kernel writes raw partial products (alpha = 1,
     // beta = 0) into dense workspace slices, m fastest; the reduction sums
     // them in FP64 and applies the epilogue.
@@ -374,7 +394,7 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
                     pan ? ctx->panel[slot] : nullptr, pan ? ctx->panel_bytes[slot] : 0,
                     pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0,
-                    &ctx->last_path, ctx->tile_form);
+                    &ctx->last_path, form);
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -708,6 +728,12 @@ int t1m_create(t1m_context** out, int device) {
   if (cudaDeviceGetAttribute(&khz, cudaDevAttrClockRate, device) == cudaSuccess && khz > 0)
     ctx->clock_khz = khz;
   *out = ctx;
+  return T1M_OK;
+}
+
+int t1m_set_autotune(t1m_context* ctx, int on) {
+  if (!ctx) return T1M_ERR_INVALID_ARGUMENT;
+  ctx->autotune = on != 0;
   return T1M_OK;
 }
 
@@ -1205,6 +1231,115 @@ int log2_bucket(int64_t v) {
 std::string shape_class(int dtype, const HostPlan& hp) {
   return std::to_string(dtype) + ":" + std::to_string(log2_bucket(hp.M)) + "," +
          std::to_string(log2_bucket(hp.N)) + "," + std::to_string(log2_bucket(hp.K));
+}
+
+// Single tensor-core products: per shape class (dtype, method, log2 of M, N,
+// K, which operand directions have unit stride), the tile form (one CTA or
+// CTA pairs) and the split count (the heuristic one, half or twice it, never
+// below the precision rule's minimum) that ran fastest, measured once on
+// the call's own operands into scratch outputs (the split workspace: the
+// partials and a dense M x N result), three runs each after a warm-up.
+// Choice code: form * 100 + split variant.
+bool tuned_product(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
+                   const GemmArgs& g, cudaStream_t s, int slot, int* form, int* splits,
+                   int64_t* k_per_split) {
+  int bm, bn, bk;
+  tc_tile(dtype, &bm, &bn, &bk);
+  const int64_t ksteps = (g.K + bk - 1) / bk;
+  int64_t kps0 = 0;
+  const int s0 = choose_splits(ctx, method, dtype, g.M, g.N, g.K, es, &kps0,
+                               ctx->method == T1M_METHOD_AUTO);
+  const int64_t lim = ctx->method == T1M_METHOD_AUTO ? accuracy_k_limit(method, dtype) : 0;
+  const int64_t smin = lim > 0 ? (g.K + lim - 1) / lim : 1;
+  auto variant = [&](int v) {
+    int64_t sp = v == 0 ? s0 : v == 1 ? (s0 + 1) / 2 : 2 * int64_t(s0);
+    sp = std::max<int64_t>({sp, smin, 1});
+    sp = std::min<int64_t>({sp, ksteps, 4096});
+    while (sp > 1 && size_t(sp + 1) * size_t(g.M) * size_t(g.N) * es > kMaxWorkBytes) --sp;
+    const int64_t steps_per = (ksteps + sp - 1) / sp;
+    *k_per_split = steps_per * bk;
+    return static_cast<int>((ksteps + steps_per - 1) / steps_per);
+  };
+  const std::string key = "s:" + std::to_string(dtype) + ":" + std::to_string(method) + ":" +
+                          std::to_string(log2_bucket(g.M)) + "," + std::to_string(log2_bucket(g.N)) +
+                          "," + std::to_string(log2_bucket(g.K)) + ":" +
+                          std::to_string(int(hp.uA_m == 1)) + std::to_string(int(hp.uA_k == 1)) +
+                          std::to_string(int(hp.uB_k == 1)) + std::to_string(int(hp.uB_n == 1));
+  std::lock_guard<std::mutex> lock(g_tune.mu);
+  g_tune.load(ctx->device);
+  auto it = g_tune.choice.find(key);
+  int code = -1;
+  if (it != g_tune.choice.end()) {
+    code = it->second;
+  } else {
+    float best = 1e30f;
+    for (int f : {T1M_TILE_ONE, T1M_TILE_PAIR}) {
+      int last_sp = -1;
+      for (int v = 0; v < 3; ++v) {
+        const int sp = variant(v);
+        const int64_t kps = *k_per_split;
+        if (sp == last_sp) continue;
+        last_sp = sp;
+        const size_t need = size_t(sp + 1) * size_t(g.M) * size_t(g.N) * es;
+        if (ensure_work(ctx, need) != T1M_OK) return false;
+        char* work = static_cast<char*>(ctx->work);
+        // Raw partials (or the one dense result) into the workspace; the
+        // reduction writes a dense M x N scratch after them.
+        GemmArgs gm = g;
+        gm.C = work;
+        gm.rsC = gm.csC = nullptr;
+        gm.uC_m = 1;
+        gm.uC_n = g.M;
+        gm.alpha[0] = 1.0;
+        gm.alpha[1] = 0.0;
+        gm.beta[0] = gm.beta[1] = 0.0;
+        gm.flags = (g.flags & (kFlagConjA | kFlagConjB)) | kFlagBetaZero;
+        gm.k_per_split = sp > 1 ? kps : g.K;
+        gm.c_split_stride = sp > 1 ? g.M * g.N : 0;
+        GemmArgs red = gm;
+        red.C = work + size_t(sp) * size_t(g.M) * size_t(g.N) * es;
+        const size_t pb = tc_panel_bytes(dtype, gm.M, gm.N, gm.K);
+        const bool pan = pb > 0 && (ctx->opt_work_limit < 0 || pb <= size_t(ctx->opt_work_limit)) &&
+                         ensure_opt_work(s, &ctx->panel[slot], &ctx->panel_bytes[slot], pb);
+        const size_t kb = tc_pack_bytes(dtype, hp);
+        const bool pk = kb > 0 && (ctx->opt_work_limit < 0 || kb <= size_t(ctx->opt_work_limit)) &&
+                        ensure_opt_work(s, &ctx->pack[slot], &ctx->pack_bytes[slot], kb);
+        float total = 0;
+        bool ok = true;
+        for (int rep = 0; rep < 4 && ok; ++rep) {
+          cudaEventRecord(ctx->ev[4], s);
+          int nk = 0, ran = method;
+          std::string err;
+          cudaError_t e = launch_tc(method, dtype, gm, hp, sp, s, ctx->d_err, &nk, &err, &ran,
+                                    pan ? ctx->panel[slot] : nullptr,
+                                    pan ? ctx->panel_bytes[slot] : 0,
+                                    pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0,
+                                    nullptr, f);
+          if (e == cudaSuccess && sp > 1) e = launch_splitk_reduce(dtype, work, sp, red, s);
+          cudaEventRecord(ctx->ev[5], s);
+          if (e != cudaSuccess || cudaEventSynchronize(ctx->ev[5]) != cudaSuccess) {
+            cudaGetLastError();
+            ok = false;
+            break;
+          }
+          float ms = 0;
+          cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+          if (rep > 0) total += ms;  // the first run warms up
+        }
+        if (ok && total < best) {
+          best = total;
+          code = f * 100 + v;
+        }
+      }
+    }
+    if (code < 0) return false;
+    if (check_device_error(ctx) != T1M_OK) return false;
+    g_tune.choice[key] = code;
+    g_tune.save();
+  }
+  *form = code / 100;
+  *splits = variant(code % 100);
+  return true;
 }
 
 // Default family before (or without) tuning.
