@@ -1242,6 +1242,13 @@ template <int AMode, int BMode, int Prec, bool kReal, bool kPair>
 __global__ void __launch_bounds__(kThreads1, 1)
 tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
   constexpr bool kBF16 = Prec != kPrecTF32x3;
+  // Stages per main chunk: the truncation bias of the tensor cores' FP32
+  // accumulation grows with the accumulating MMAs per chunk, so chunks hold
+  // 16 main-product MMAs: 8 stages of 2 kind::f16 MMAs (K = 16) or 4 of 4
+  // kind::tf32 MMAs (K = 8).  Measured at complex64 4096^3: BF16x6 folding
+  // every 8 stages 221.5 -> 225.5 TFLOP/s, error 2.8e-7 -> 3.3e-7 (log-uniform
+  // set 3.2e-7 -> 3.6e-7); 3xTF32 at 8 stages rose to 6.9e-7, so it keeps 4.
+  constexpr int kFoldT = kBF16 ? 2 * kFold : kFold;
   constexpr int kPieces = Prec == kPrecBF16x6 ? 3 : 2;
   // MMA M: 128 real rows per CTA, 256 for a pair.
   constexpr uint32_t kIdescT = ptx::idesc_f32acc(kBF16 ? 1u /*BF16*/ : 2u /*TF32*/,
@@ -1402,9 +1409,9 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       for (int64_t s = 0; s < ksteps; ++s) {
         const int st = static_cast<int>(s % kStages);
         const uint32_t ph = static_cast<uint32_t>((s / kStages) & 1);
-        const int64_t c = s / kFold;
+        const int64_t c = s / kFoldT;
         const int buf = static_cast<int>(c & 1);
-        const bool chunk_start = (s % kFold) == 0;
+        const bool chunk_start = (s % kFoldT) == 0;
         if (issue_main && chunk_start && c >= 2 &&
             !wait_conv(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
           record_error(err_flag, kErrChunkWait);
@@ -1463,7 +1470,7 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
         }
         commit(empty_bar(st));
         if (kPanel) commit(pempty(sb));
-        if (issue_main && ((s % kFold) == kFold - 1 || s == ksteps - 1)) commit(chunk_full(buf));
+        if (issue_main && ((s % kFoldT) == kFoldT - 1 || s == ksteps - 1)) commit(chunk_full(buf));
       }
       // Signal the epilogue (also after an abort, so nobody waits forever),
       // then make sure no MMA is still writing TMEM before it is freed.
@@ -1777,8 +1784,8 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       // covered the MMAs of stage 4 c + 3 (the chunk's last), so the chunk
       // wait does not stall the next conversion.  The chunk's buffer is next
       // written by chunk c + 2, from stage 4 (c + 2).
-      if ((s % kFold) == 1 && s > kFold) {
-        const int64_t c = s / kFold - 1;
+      if ((s % kFoldT) == 1 && s > kFoldT) {
+        const int64_t c = s / kFoldT - 1;
         const int buf = static_cast<int>(c & 1);
         if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
           record_error(err_flag, kErrChunkWait);
@@ -1810,8 +1817,8 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
     if (ok) {
       // Chunks the loop did not fold: the last, and the one before it when
       // the last has a single stage; then add the corrections.
-      const int64_t c_last = (ksteps - 1) / kFold;
-      if (c_last >= 1 && ksteps < kFold * c_last + 2)
+      const int64_t c_last = (ksteps - 1) / kFoldT;
+      if (c_last >= 1 && ksteps < kFoldT * c_last + 2)
         fold_from(((c_last - 1) & 1) ? kChunkCol1 : kChunkCol0);
       fold_from((c_last & 1) ? kChunkCol1 : kChunkCol0);
       fold_from(kCorrCol);
