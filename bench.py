@@ -347,6 +347,18 @@ def run_gpu(args) -> None:
         rep = t1m.contract_raw(1.0, hta, LA, htb, LB, 0.0, htc, LC, t1m.FLAG_NO_TIMING, ctx)
         h2d, d2h = rep.h2d_bytes, rep.d2h_bytes
     e2e_s = (time.perf_counter() - t0) / e2e_steps
+    # The same with pageable host buffers (what a C++ caller holding
+    # std::vector data passes): the copies go through the driver's staging
+    # and overlap the kernels less.
+    pa, pb = ha.numpy().copy(), hb.numpy().copy()
+    pc = np.empty(M * N, dtype=np.complex64)
+    pta, ptb, ptc = t1m.tensor(dims, pa), t1m.tensor(dims, pb), t1m.tensor(dims, pc)
+    t1m.contract_raw(1.0, pta, LA, ptb, LB, 0.0, ptc, LC, t1m.FLAG_NO_TIMING, ctx)
+    page_steps = max(1, min(args.steps, 5))
+    t0 = time.perf_counter()
+    for _ in range(page_steps):
+        t1m.contract_raw(1.0, pta, LA, ptb, LB, 0.0, ptc, LC, t1m.FLAG_NO_TIMING, ctx)
+    e2e_page_s = (time.perf_counter() - t0) / page_steps
 
     # Max over ranks.
     vals = torch.tensor([ms_tc, ms_plain, e2e_s], dtype=torch.float64, device=dev)
@@ -358,6 +370,9 @@ def run_gpu(args) -> None:
         step_ms = ms_tc / args.steps
         value = world * FLOPS / (step_ms * 1e-3) / 1e12
         plain_tflops = FLOPS / (ms_plain / plain_steps * 1e-3) / 1e12
+        # FP32 SIMT nominal: 152 SMs x 128 FMA lanes x 2 flop x max SM clock
+        # (no measured FP32 peak exists).
+        fp32_nominal = 152 * 128 * 2 * peaks.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
         per_gpu = FLOPS / (step_ms * 1e-3) / 1e12
         kernel_tflops = FLOPS / (kernel_ms * 1e-3) / 1e12
         if tc_method == "tc_3xtf32":
@@ -384,7 +399,9 @@ def run_gpu(args) -> None:
                        "l2": "inputs larger than L2 (A, B, C 134 MB each)",
                        "parallelism": f"replicas x{world}"},
             "plain_fp32": {"value": plain_tflops, "unit": "TFLOP/s", "steps": plain_steps,
-                           "rel_err_max": err_plain[0], "rel_err_fro": err_plain[1]},
+                           "rel_err_max": err_plain[0], "rel_err_fro": err_plain[1],
+                           "frac_of_fp32_simt_nominal": plain_tflops / fp32_nominal,
+                           "fp32_simt_nominal_tflops": fp32_nominal},
             "speedup_vs_plain": per_gpu / plain_tflops,
             "other_tc_methods": other,
             "rel_err": {"max": err_tc[0], "fro": err_tc[1],
@@ -397,7 +414,10 @@ def run_gpu(args) -> None:
                                            "read+write per launch)",
                          "peak_note": peak_note},
             "e2e": {"value": world * FLOPS / e2e_s / 1e12, "unit": "TFLOP/s",
-                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "host_buffers": "pinned",
+                    "pageable": {"value": FLOPS / e2e_page_s / 1e12, "unit": "TFLOP/s",
+                                 "steps": page_steps, "rank": rank}},
             "gpu_launches": int(launches),
             "clocks": clocks,
         }
