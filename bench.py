@@ -59,10 +59,9 @@ def _peaks() -> dict:
             "sm_max_mhz": 2070.0, "_source": "fallback"}
 
 
-# ncu summaries of the dominant kernel per method (CTA-pair form for BF16x6,
-# the automatic tile form of this workload; the 3xTF32 summary is of the
-# one-CTA form with B panels).
-PROFILE_OF = {"tc_3xtf32": "tc1m_contract_ijkl_klmn_64.md",
+# ncu summaries of the dominant kernel per method (the CTA-pair form, the
+# automatic tile form of this workload).
+PROFILE_OF = {"tc_3xtf32": "tc1m_contract_pair_3xtf32_ijkl_klmn_64.md",
               "tc_bf16x6": "tc1m_contract_pair_bf16x6_ijkl_klmn_64.md"}
 
 
