@@ -444,12 +444,21 @@ __device__ __forceinline__ void skinny_body(const GemmArgs& g, int64_t tile, T (
 // stride): the CTA's 32 rows stream through a ring of kSkStages shared-memory
 // stages of 64 k with cp.async (16 bytes per copy, zero fill past the edges),
 // so the loads in flight no longer depend on registers; B's whole K chunk
-// (at most kSkinnyAsyncMaxK) is staged once.  Warp w reduces rows 4w..4w+3,
-// lanes over k as in skinny_body.
-constexpr int kSkStages = 3;
+// (at most kSkinnyAsyncMaxK) is staged once, after the first A stages are
+// issued.  Warp w reduces rows 4w..4w+3, lanes over k as in skinny_body.
+// Five stages of 16 KB with two CTAs per SM keep up to 128 KB of A in flight
+// per SM; the sweep's second steps (59.8 GB of A per batch) read at 2.8 TB/s,
+// about as with three stages: the per-tile B staging and the short K chunks
+// (at most kSkinnyAsyncMaxK per tile) bound them.
+constexpr int kSkStages = 5;
 constexpr int kSkKS = 64;  // k per stage
 constexpr size_t kSkAsyncSmem =
-    size_t(kSkStages) * 32 * kSkKS * 8 + size_t(4) * kSkinnyAsyncMaxK * 8;  // 80 KB
+    size_t(kSkStages) * 32 * kSkKS * 8 + size_t(4) * kSkinnyAsyncMaxK * 8;  // 112 KB
+// Shared memory of the generic skinny body (B chunk and its K offsets).
+template <class T, int NMAX>
+constexpr size_t skinny_generic_smem() {
+  return size_t(NMAX) * (2048 / NMAX) * sizeof(T) + size_t(2048 / NMAX) * sizeof(int64_t);
+}
 
 __device__ __forceinline__ void cp_async_16(uint32_t dst, const void* src, uint32_t src_bytes) {
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src),
@@ -487,14 +496,6 @@ __device__ __forceinline__ void skinny_async_body(const GemmArgs& g, int64_t til
   const bool conjB = g.flags & kFlagConjB;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
-  // B chunk, zero-padded to NMAX columns and to whole stages.
-  for (int e = tid; e < NMAX * nst * kSkKS; e += kThreads) {
-    const int n = e / (nst * kSkKS), kk = e % (nst * kSkKS);
-    T v = zero<T>();
-    if (n < N && kk < kn)
-      v = conj_if(B[offs(g.rsB, g.uB_k, kb + kk) + offs(g.csB, g.uB_n, n)], conjB);
-    Bs[n][kk] = v;
-  }
   // Copies of this thread: 16-byte chunk c = tid + 256 i of a stage, row
   // c / 32, elements 2 (c % 32) and 2 (c % 32) + 1.
   int64_t rowoff[4];
@@ -524,6 +525,15 @@ __device__ __forceinline__ void skinny_async_body(const GemmArgs& g, int64_t til
   for (int s = 0; s < kSkStages - 1; ++s) {
     if (s < nst) issue(s);
     else cp_async_commit();
+  }
+  // B chunk, zero-padded to NMAX columns and to whole stages, while the
+  // first A stages are in flight (visible at the first stage's barrier).
+  for (int e = tid; e < NMAX * nst * kSkKS; e += kThreads) {
+    const int n = e / (nst * kSkKS), kk = e % (nst * kSkKS);
+    T v = zero<T>();
+    if (n < N && kk < kn)
+      v = conj_if(B[offs(g.rsB, g.uB_k, kb + kk) + offs(g.csB, g.uB_n, n)], conjB);
+    Bs[n][kk] = v;
   }
   T acc[RW][NMAX];
 #pragma unroll
@@ -569,9 +579,11 @@ template <class T, int NMAX>
 __global__ void __launch_bounds__(kThreads)
 skinny_contract(const SimtProblem* group, int nprob) {
   __shared__ GemmArgs ga;
-  __shared__ __align__(16) T Bs[NMAX][2048 / NMAX];
-  __shared__ int64_t ks[2048 / NMAX];
+  // One dynamic area serves either body: the asynchronous ring and B chunk,
+  // or the generic body's B chunk and K offsets.
   extern __shared__ __align__(16) unsigned char skinny_dsmem[];
+  T (*Bs)[2048 / NMAX] = reinterpret_cast<T (*)[2048 / NMAX]>(skinny_dsmem);
+  int64_t* ks = reinterpret_cast<int64_t*>(skinny_dsmem + size_t(NMAX) * (2048 / NMAX) * sizeof(T));
   int64_t tile = blockIdx.x;
   int lo = 0, hi = nprob - 1;
   while (lo < hi) {
@@ -598,10 +610,11 @@ cudaError_t launch_skinny(const SimtProblem* dev, int nprob, int64_t total_tiles
                           cudaStream_t stream) {
   if (total_tiles <= 0) return cudaSuccess;
   if (total_tiles > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  // The asynchronous form's ring and B chunk (dynamic shared memory) exist
-  // only in the instances that can run it.
-  constexpr size_t kDyn = (NMAX == 4 && sizeof(T) == 8) ? kSkAsyncSmem : 0;
-  if constexpr (kDyn > 0) {
+  // The asynchronous form's ring and B chunk exist only in the instances
+  // that can run it; the generic body's arrays share the same area.
+  constexpr size_t kGen = skinny_generic_smem<T, NMAX>();
+  constexpr size_t kDyn = (NMAX == 4 && sizeof(T) == 8 && kSkAsyncSmem > kGen) ? kSkAsyncSmem : kGen;
+  if constexpr (kDyn > 48 * 1024) {
     static bool attr_set = false;
     if (!attr_set) {
       const cudaError_t e = cudaFuncSetAttribute(
