@@ -718,8 +718,9 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--method", default="auto")
-    ap.add_argument("--tile-form", default="auto", choices=["auto", "one", "pair"],
-                    help="tensor-core tile form (one tile per CTA or CTA pairs)")
+    ap.add_argument("--tile-form", default="auto", choices=["auto", "one", "pair", "pieces"],
+                    help="tensor-core tile form (one tile per CTA, CTA pairs, or CTA pairs "
+                         "over operands split into bf16 pieces beforehand)")
     ap.add_argument("--autotune", action="store_true",
                     help="tune tile form and split count per shape class (first call)")
     ap.add_argument("--no-cpu-baseline", action="store_true")

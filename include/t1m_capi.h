@@ -114,6 +114,8 @@ typedef struct t1m_report {
 #define T1M_PATH_A_PACKED 0x200
 #define T1M_PATH_B_PACKED 0x400
 #define T1M_PATH_B_PANELS 5
+#define T1M_PATH_PIECES 0x2000    /* CTA pairs over operands split into bf16
+                                     pieces beforehand (T1M_TILE_PIECES)    */
 
 typedef struct t1m_context t1m_context;
 
@@ -162,6 +164,12 @@ int t1m_set_wait_limit(t1m_context* ctx, int64_t microseconds);
 #define T1M_TILE_AUTO 0
 #define T1M_TILE_ONE 1
 #define T1M_TILE_PAIR 2
+/* CTA pairs whose MMAs read both operands from shared memory, loaded by TMA
+ * from copies split once into bf16 pieces (the bf16 methods; the copies
+ * take the optional workspace: 2P bytes per real value of the 1M-expanded A
+ * and of B, P = 3 pieces for BF16x6, 2 for BF16x3).  Same results as
+ * T1M_TILE_PAIR, bit for bit.  Elsewhere it runs as T1M_TILE_PAIR. */
+#define T1M_TILE_PIECES 3
 int t1m_set_tile_form(t1m_context* ctx, int form);
 /* Autotuning of single tensor-core contractions (on != 0; default off): per
  * shape class (element type, method, log2 of M, N and K, which operand

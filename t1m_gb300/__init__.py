@@ -49,8 +49,9 @@ FLAG_NO_TIMING = 8
 # t1m_report.path (T1M_PATH_* of t1m_capi.h)
 PATH_TC, PATH_PERSISTENT, PATH_A_PACKED, PATH_B_PACKED = 0x1000, 0x100, 0x200, 0x400
 PATH_PAIR = 0x800
+PATH_PIECES = 0x2000
 # t1m_set_tile_form
-TILE_FORMS = {"auto": 0, "one": 1, "pair": 2}
+TILE_FORMS = {"auto": 0, "one": 1, "pair": 2, "pieces": 3}
 A_MODES = {0: "gather", 1: "MK", 2: "MK16", 3: "KM", 4: "KM16", 5: "MK16K"}
 B_MODES = {0: "gather", 1: "NK", 2: "KN", 3: "NK16", 4: "KN16", 5: "panels"}
 
@@ -106,7 +107,7 @@ class Report(C.Structure):
             return None
         return {"a": A_MODES[p & 15], "b": B_MODES[(p >> 4) & 15],
                 "persistent": bool(p & PATH_PERSISTENT), "pair": bool(p & PATH_PAIR),
-                "a_packed": bool(p & PATH_A_PACKED),
+                "pieces": bool(p & PATH_PIECES), "a_packed": bool(p & PATH_A_PACKED),
                 "b_packed": bool(p & PATH_B_PACKED)}
 
 

@@ -385,7 +385,10 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       const auto within = [&](size_t bytes) {
         return ctx->opt_work_limit < 0 || bytes <= static_cast<size_t>(ctx->opt_work_limit);
       };
-      const size_t pb = tc_panel_bytes(dtype, gm.M, gm.N, gm.K);
+      const size_t pb = std::max(tc_panel_bytes(dtype, gm.M, gm.N, gm.K),
+                                 form == T1M_TILE_PIECES
+                                     ? tc_pieces_bytes(dtype, method, gm.M, gm.N, gm.K)
+                                     : size_t(0));
       const bool pan = pb > 0 && within(pb) &&
                        ensure_opt_work(s, &ctx->panel[slot], &ctx->panel_bytes[slot], pb);
       const size_t kb = tc_pack_bytes(dtype, hp);
@@ -744,7 +747,7 @@ int t1m_set_wait_limit(t1m_context* ctx, int64_t microseconds) {
 }
 
 int t1m_set_tile_form(t1m_context* ctx, int form) {
-  if (!ctx || form < T1M_TILE_AUTO || form > T1M_TILE_PAIR) return T1M_ERR_INVALID_ARGUMENT;
+  if (!ctx || form < T1M_TILE_AUTO || form > T1M_TILE_PIECES) return T1M_ERR_INVALID_ARGUMENT;
   ctx->tile_form = form;
   return T1M_OK;
 }
@@ -1298,7 +1301,10 @@ bool tuned_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
         gm.c_split_stride = sp > 1 ? g.M * g.N : 0;
         GemmArgs red = gm;
         red.C = work + size_t(sp) * size_t(g.M) * size_t(g.N) * es;
-        const size_t pb = tc_panel_bytes(dtype, gm.M, gm.N, gm.K);
+        const size_t pb = std::max(tc_panel_bytes(dtype, gm.M, gm.N, gm.K),
+                                   f == T1M_TILE_PIECES
+                                       ? tc_pieces_bytes(dtype, method, gm.M, gm.N, gm.K)
+                                       : size_t(0));
         const bool pan = pb > 0 && (ctx->opt_work_limit < 0 || pb <= size_t(ctx->opt_work_limit)) &&
                          ensure_opt_work(s, &ctx->panel[slot], &ctx->panel_bytes[slot], pb);
         const size_t kb = tc_pack_bytes(dtype, hp);

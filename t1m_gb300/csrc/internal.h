@@ -210,6 +210,10 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                       int* path = nullptr, int form = 0 /* T1M_TILE_* */);
 // Panel workspace a product would use (0: panels not used at this size).
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K);
+// Bytes of the operand pieces of the T1M_TILE_PIECES form (held in the panel
+// workspace), 0 where that form does not apply.  kMethodTcAuto counts the
+// BF16x6 pieces.
+size_t tc_pieces_bytes(int dtype, int method, int64_t M, int64_t N, int64_t K);
 // Pack workspace a product may use (0: neither operand would be packed).
 size_t tc_pack_bytes(int dtype, const HostPlan& plan);
 

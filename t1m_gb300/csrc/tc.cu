@@ -1845,6 +1845,343 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
   }
 }
 
+// ------------------------------------------------------ operand pieces ---
+// CTA pairs over operands split into bf16 pieces beforehand.
+//
+// A pre-pass (split_pieces) writes, for every complex row m of A, the two 1M
+// rows [re, -im, ...] and [im, re, ...] and, for every column n of B, the row
+// [re, im, ...] of its complex k (K fastest, real k = 2k + part), each value
+// split into P bf16 pieces exactly as tc1m_contract's converters split them
+// (split_bf16, conjugation first): P arrays per operand, rows `pitch`
+// elements apart.  The pair kernel then runs without converters: TMA loads
+// all pieces of a stage (3-D boxes: 64 real k x rows x P) into 128-byte
+// swizzled K-major shared memory, and one thread of the even CTA issues
+// tcgen05.mma.cta_group::2 with both operands read from shared memory.
+// Per accumulator its MMAs run in tc1m_contract's order (main product into
+// the chunk accumulators, a chunk every 16 MMAs of K = 16; corrections x0y1,
+// x1y0 [, x1y1, x0y2, x2y0] per K = 16 step into their own accumulator), so
+// the two forms give the same result bit for bit.
+//
+// The split happens once per operand element instead of once per tile that
+// reads it; the price is the pieces in device memory: 2 x 2 x 2P bytes per
+// complex element of A (the 1M rows) and 2 x 2P per element of B, written
+// and read back once by TMA per tile.
+constexpr int kPcStepK = 64;                   // real k per stage: one 128-byte row per piece
+constexpr int kPcABytes = 128 * 128;           // one A piece of a stage: 128 real rows
+constexpr int kPcBBytes = (kTileN / 2) * 128;  // one B piece: this CTA's 64 columns
+constexpr int kPcFold = 4;                     // stages per main chunk (16 MMAs of K = 16)
+constexpr int kPcBarrierBytes = 256;
+template <int P>
+constexpr int pc_stage_bytes() {
+  return P * (kPcABytes + kPcBBytes);
+}
+// Stages in the ring: as many as 227 KB hold (72 KB each for three pieces).
+template <int P>
+constexpr int pc_stages() {
+  return P == 3 ? 3 : 4;
+}
+template <int P>
+constexpr int pc_smem_bytes() {
+  return 1024 + pc_stages<P>() * pc_stage_bytes<P>() + kPcBarrierBytes;
+}
+
+// Pieces of one operand for a block of 32 rows x 32 complex k (256 threads):
+// the block reads its tile along whichever direction has unit stride
+// (through the offset vectors otherwise) and writes 16 bytes per piece and
+// output row per thread (4 complex k).  Blocks [0, blocks_a) cover A,
+// the rest B.  Rows past M or N are not written (the tensor maps end
+// there); complex k in [K, K rounded up to 4) are written as zeros.
+template <int P>
+__global__ void __launch_bounds__(256)
+split_pieces(const GemmArgs g, uint16_t* __restrict__ pa, uint16_t* __restrict__ pb,
+             int64_t pitch, int64_t plane_a, int64_t plane_b, int64_t blocks_a, int64_t tiles_k) {
+  __shared__ float2 tile[32][33];
+  const bool is_a = blockIdx.x < blocks_a;
+  const int64_t bid = is_a ? blockIdx.x : blockIdx.x - blocks_a;
+  const int64_t r0 = (bid / tiles_k) * 32, k0 = (bid % tiles_k) * 32;
+  const int64_t R = is_a ? g.M : g.N, K = g.K;
+  const float2* __restrict__ src = static_cast<const float2*>(is_a ? g.A : g.B);
+  const int64_t* rs = is_a ? g.rsA : g.csB;
+  const int64_t* ks = is_a ? g.csA : g.rsB;
+  const int64_t ur = is_a ? g.uA_m : g.uB_n;
+  const int64_t uk = is_a ? g.uA_k : g.uB_k;
+  const bool row_fast = ur == 1 && uk != 1;
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int r = row_fast ? (t & 31) : (t >> 5) + 8 * i;
+    const int k = row_fast ? (t >> 5) + 8 * i : (t & 31);
+    float2 v = make_float2(0.f, 0.f);
+    if (r0 + r < R && k0 + k < K) v = src[offs(rs, ur, r0 + r) + offs(ks, uk, k0 + k)];
+    tile[r][k] = v;
+  }
+  __syncthreads();
+  const int r = t >> 3, kq = 4 * (t & 7);
+  if (r0 + r >= R || k0 + kq >= K) return;
+  const bool conj = g.flags & (is_a ? kFlagConjA : kFlagConjB);
+  float2 v[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    v[j] = tile[r][kq + j];
+    if (conj) v[j].y = -v[j].y;
+  }
+  const int64_t col = 2 * (k0 + kq);
+  uint32_t w[3][4];
+  if (is_a) {
+#pragma unroll
+    for (int part = 0; part < 2; ++part) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float x0 = part ? v[j].y : v[j].x;
+        const float x1 = part ? v[j].x : -v[j].y;
+        split_bf16<P>(x0, x1, w[0][j], w[1][j], w[2][j]);
+      }
+      uint16_t* row = pa + (2 * (r0 + r) + part) * pitch + col;
+#pragma unroll
+      for (int p = 0; p < P; ++p)
+        *reinterpret_cast<uint4*>(row + p * plane_a) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) split_bf16<P>(v[j].x, v[j].y, w[0][j], w[1][j], w[2][j]);
+    uint16_t* row = pb + (r0 + r) * pitch + col;
+#pragma unroll
+    for (int p = 0; p < P; ++p)
+      *reinterpret_cast<uint4*>(row + p * plane_b) = make_uint4(w[p][0], w[p][1], w[p][2], w[p][3]);
+  }
+}
+
+// The pair kernel over pieces.  Warps: 0 TMEM allocation and (even CTA, one
+// lane) MMA issue; 1 TMA (one lane per CTA); 2 (odd CTA, one lane) relays
+// the arrival of its stage to the even CTA's MMA thread; 4-11 fold the chunk
+// accumulators and write C (two warpgroups of 64 columns each, one TMEM lane
+// per thread), as tc1m_contract's converters do.
+template <int Prec>
+__global__ void __launch_bounds__(kThreads1, 1)
+tc1m_pieces(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* err_flag) {
+  constexpr int P = Prec == kPrecBF16x6 ? 3 : 2;
+  constexpr int S = pc_stages<P>();
+  constexpr int kStageB = pc_stage_bytes<P>();
+  constexpr uint32_t kIdescP = ptx::idesc_f32acc(1u /*BF16*/, 256u, kTileN);
+  static_assert(8 * (3 * S + 6) <= kPcBarrierBytes, "barrier area");
+  static_assert(kStageB % 1024 == 0 && kPcBBytes % 1024 == 0, "swizzle atoms");
+
+  extern __shared__ __align__(16) uint8_t smem_raw[];
+  const uint32_t base = (ptx::smem_u32(smem_raw) + 1023u) & ~1023u;
+  uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
+  const uint32_t bars = base + S * kStageB;
+  auto full_bar = [&](int s) { return bars + 8u * s; };
+  auto peer_bar = [&](int s) { return bars + 8u * (S + s); };
+  auto empty_bar = [&](int s) { return bars + 8u * (2 * S + s); };
+  auto chunk_full = [&](int b) { return bars + 8u * (3 * S + b); };
+  auto chunk_empty = [&](int b) { return bars + 8u * (3 * S + 2 + b); };
+  const uint32_t acc_bar = bars + 8u * (3 * S + 4);
+  const uint32_t tmem_slot = acc_bar + 8u;
+  volatile uint32_t* tmem_slot_ptr =
+      reinterpret_cast<volatile uint32_t*>(base_ptr + (tmem_slot - base));
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const uint32_t rank = ptx::cluster_ctarank();
+  if (warp == 0) {
+    ptx::tmem_alloc2(tmem_slot, kTmemCols);
+    ptx::tmem_relinquish2();
+  }
+  if (tid == 32) {
+    for (int s = 0; s < S; ++s) {
+      ptx::mbar_init(full_bar(s), 1);
+      ptx::mbar_init(peer_bar(s), 1);
+      ptx::mbar_init(empty_bar(s), 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      ptx::mbar_init(chunk_full(b), 1);
+      ptx::mbar_init(chunk_empty(b), 2 * (kConverters1 / 32));
+    }
+    ptx::mbar_init(acc_bar, 1);
+    ptx::fence_mbar_init();
+  }
+  if (tid == 64) {
+    ptx::tma_prefetch_desc(&maps.a);
+    ptx::tma_prefetch_desc(&maps.b);
+  }
+  ptx::tc_fence_before();
+  ptx::cluster_sync();
+  ptx::tc_fence_after();
+  const uint32_t tmem = *tmem_slot_ptr;
+
+  // Tiles as in tc1m_contract's pair form: groups of 8 pair tiles along M
+  // sweep N; split-K rows over blockIdx.y.
+  const int64_t M = args.M, N = args.N;
+  const int64_t kb = static_cast<int64_t>(blockIdx.y) * args.k_per_split;
+  const int64_t K = min(args.K, kb + args.k_per_split);
+  constexpr int kRowsTile = 2 * kTileMc;
+  const int64_t tiles_m = (M + kRowsTile - 1) / kRowsTile;
+  const int64_t tiles_n = (N + kTileN - 1) / kTileN;
+  constexpr int64_t G = 8;
+  const int64_t t = blockIdx.x >> 1;
+  const int64_t group = t / (G * tiles_n);
+  const int64_t first_m = group * G;
+  const int64_t gsize = min(G, tiles_m - first_m);
+  const int64_t tm = first_m + (t % (G * tiles_n)) % gsize;
+  const int64_t tn = (t % (G * tiles_n)) / gsize;
+  const int64_t m0 = tm * kRowsTile + rank * kTileMc, n0 = tn * kTileN;
+  // Stages of 64 real k over this CTA row's real K range [2 kb, 2 K).
+  const int64_t ksteps = (2 * (K - kb) + kPcStepK - 1) / kPcStepK;
+
+  if (warp == 0) {
+    // ---------------------------------------------------------- MMA issue ---
+    if (lane == 0 && rank == 0) {
+      const uint64_t desc0 = ptx::smem_desc_sw128(base);
+      const uint32_t d_corr = tmem + kCorrCol;
+      for (int64_t s = 0; s < ksteps; ++s) {
+        const int st = static_cast<int>(s % S);
+        const uint32_t ph = static_cast<uint32_t>((s / S) & 1);
+        const int64_t c = s / kPcFold;
+        const int buf = static_cast<int>(c & 1);
+        const bool chunk_start = (s % kPcFold) == 0;
+        if (chunk_start && c >= 2 &&
+            !ptx::mbar_wait(chunk_empty(buf), static_cast<uint32_t>(((c - 2) >> 1) & 1))) {
+          record_error(err_flag, kErrChunkWait);
+          break;
+        }
+        if (!ptx::mbar_wait(full_bar(st), ph) || !ptx::mbar_wait(peer_bar(st), ph)) {
+          record_error(err_flag, kErrFullWait);
+          break;
+        }
+        ptx::tc_fence_after();
+        const uint32_t d_main = tmem + (buf ? kChunkCol1 : kChunkCol0);
+        const uint64_t ds = desc0 + static_cast<uint64_t>((st * kStageB) >> 4);
+        // K = 16 steps of this stage inside the CTA row's K range: a split
+        // may end half way through a stage (its K a multiple of 16 complex);
+        // the rest of the box belongs to the next split.  Past the end of K
+        // the box is zero-filled.
+        const int64_t rem = 2 * (K - kb) - kPcStepK * s;
+        const int nkk = rem >= kPcStepK ? 4 : static_cast<int>((rem + 15) / 16);
+        // Piece p, K = 16 step kk: A at +p x 16 KB, B after the A pieces at
+        // +p x 8 KB, each +32 bytes per step inside the 128-byte rows.
+        auto da = [&](int p, int kk) {
+          return ds + static_cast<uint64_t>((p * kPcABytes + 32 * kk) >> 4);
+        };
+        auto db = [&](int p, int kk) {
+          return ds + static_cast<uint64_t>((P * kPcABytes + p * kPcBBytes + 32 * kk) >> 4);
+        };
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk)
+          if (kk < nkk)
+            ptx::mma_f16_ss2(d_main, da(0, kk), db(0, kk), kIdescP,
+                             (chunk_start && kk == 0) ? 0u : 1u);
+#pragma unroll
+        for (int kk = 0; kk < 4; ++kk) {
+          if (kk >= nkk) break;
+          ptx::mma_f16_ss2(d_corr, da(0, kk), db(1, kk), kIdescP, (s == 0 && kk == 0) ? 0u : 1u);
+          ptx::mma_f16_ss2(d_corr, da(1, kk), db(0, kk), kIdescP, 1u);
+          if (P == 3) {
+            ptx::mma_f16_ss2(d_corr, da(1, kk), db(1, kk), kIdescP, 1u);
+            ptx::mma_f16_ss2(d_corr, da(0, kk), db(2, kk), kIdescP, 1u);
+            ptx::mma_f16_ss2(d_corr, da(2, kk), db(0, kk), kIdescP, 1u);
+          }
+        }
+        ptx::mma_commit2(empty_bar(st));
+        if ((s % kPcFold) == kPcFold - 1 || s == ksteps - 1) ptx::mma_commit2(chunk_full(buf));
+      }
+      // Signal the epilogue (also after an abort), then make sure no MMA is
+      // still writing TMEM before it is freed.
+      ptx::mma_commit2(acc_bar);
+      if (!ptx::mbar_wait(acc_bar, 0)) record_error(err_flag, kErrAccWait);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------------------------------------------------------- TMA ---
+    if (lane == 0) {
+      const int a_row = static_cast<int>(2 * m0);                   // 1M rows of this CTA
+      const int b_row = static_cast<int>(n0 + rank * (kTileN / 2));  // its B columns
+      for (int64_t s = 0; s < ksteps; ++s) {
+        const int st = static_cast<int>(s % S);
+        const uint32_t ph = static_cast<uint32_t>((s / S) & 1);
+        if (!ptx::mbar_wait(empty_bar(st), ph ^ 1u)) {
+          record_error(err_flag, kErrRawWait);
+          break;
+        }
+        const uint32_t dst = base + st * kStageB;
+        const int k0 = static_cast<int>(2 * kb + kPcStepK * s);
+        ptx::mbar_arrive_expect_tx(full_bar(st), static_cast<uint32_t>(kStageB));
+        ptx::tma_load_3d(dst, &maps.a, k0, a_row, 0, full_bar(st));
+        ptx::tma_load_3d(dst + P * kPcABytes, &maps.b, k0, b_row, 0, full_bar(st));
+      }
+    }
+    __syncwarp();
+  } else if (warp == 2) {
+    // -------------------------------------------------------------- relay ---
+    if (lane == 0 && rank == 1) {
+      for (int64_t s = 0; s < ksteps; ++s) {
+        const int st = static_cast<int>(s % S);
+        if (!ptx::mbar_wait(full_bar(st), static_cast<uint32_t>((s / S) & 1))) {
+          record_error(err_flag, kErrFullWait);
+          break;
+        }
+        ptx::mbar_arrive_cluster(ptx::mapa(peer_bar(st), 0));
+      }
+    }
+    __syncwarp();
+  } else if (tid >= kConvBase) {
+    // ------------------------------------------------- fold and epilogue ---
+    const int pt = tid - kConvBase;
+    const int wg = pt >> 7;
+    const int q = (pt >> 5) & 3;
+    const int rho = 32 * q + lane;
+    const int ci = rho >> 1;
+    const int part = rho & 1;
+    const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
+    const bool row_ok = (m0 + ci) < M;
+    float master[kMC1];
+#pragma unroll
+    for (int j = 0; j < kMC1; ++j) master[j] = 0.f;
+    auto fold_from = [&](uint32_t col) {
+#pragma unroll
+      for (int cc = 0; cc < kMC1 / 32; ++cc) {
+        uint32_t r[32];
+        ptx::tmem_ld32_sync(tmem + lane_base + col + kMC1 * wg + 32u * cc, r);
+#pragma unroll
+        for (int j = 0; j < 32; ++j) master[32 * cc + j] += __uint_as_float(r[j]);
+      }
+    };
+    bool ok = true;
+    const int64_t nchunks = (ksteps + kPcFold - 1) / kPcFold;
+    for (int64_t c = 0; c + 1 < nchunks; ++c) {
+      const int buf = static_cast<int>(c & 1);
+      if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
+        record_error(err_flag, kErrChunkWait);
+        ok = false;
+        break;
+      }
+      ptx::tc_fence_after();
+      fold_from(buf ? kChunkCol1 : kChunkCol0);
+      ptx::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) ptx::mbar_arrive_cluster(ptx::mapa(chunk_empty(buf), 0));
+    }
+    if (!ptx::mbar_wait(acc_bar, 0)) {
+      record_error(err_flag, kErrAccWait);
+      ok = false;
+    }
+    ptx::tc_fence_after();
+    if (ok) {
+      fold_from(((nchunks - 1) & 1) ? kChunkCol1 : kChunkCol0);
+      fold_from(kCorrCol);
+      float2* __restrict__ Cp =
+          static_cast<float2*>(args.C) + static_cast<int64_t>(blockIdx.y) * args.c_split_stride;
+      store_tile<kMC1>(args, Cp, m0 + ci, row_ok, n0, wg * kMC1, part, master);
+    }
+  }
+
+  ptx::tc_fence_before();
+  ptx::cluster_sync();
+  if (warp == 0) {
+    ptx::tc_fence_after();
+    ptx::tmem_dealloc2(tmem, kTmemCols);
+  }
+}
+
 // ------------------------------------------------------------------ host ---
 using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                    const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
@@ -1959,6 +2296,73 @@ cudaError_t launch_pair_prec(int method, int amode, int bmode, const GemmArgs& a
     default:
       return launch_pair<kPrecTF32x3>(amode, bmode, args, maps, stream, err_flag, tiles);
   }
+}
+
+// Operand pieces: row pitch in bf16 elements (real K rounded up to 16 bytes).
+int64_t pieces_pitch(int64_t K) { return (2 * K + 7) / 8 * 8; }
+
+// 3-D map over P piece arrays of `rows` rows of `kreal` bf16 (`pitch`
+// apart), loaded as boxes of 64 k x box_rows x P with the 128-byte swizzle.
+bool make_map_pieces(CUtensorMap* map, const void* base, int64_t kreal, int64_t rows,
+                     int64_t pitch, int pieces, uint32_t box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+  if (kreal <= 0 || rows <= 0 || kreal >= (int64_t(1) << 31) || rows >= (int64_t(1) << 31))
+    return false;
+  cuuint64_t dims[3] = {static_cast<cuuint64_t>(kreal), static_cast<cuuint64_t>(rows),
+                        static_cast<cuuint64_t>(pieces)};
+  cuuint64_t strides[2] = {static_cast<cuuint64_t>(pitch * 2),
+                           static_cast<cuuint64_t>(rows * pitch * 2)};
+  cuuint32_t box[3] = {static_cast<cuuint32_t>(kPcStepK), box_rows, static_cast<cuuint32_t>(pieces)};
+  cuuint32_t estr[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void*>(base), dims, strides, box,
+            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The pieces of A and B (one launch, counted in *kernels), then the pair
+// kernel over them: tiles.x = 2 x pair tiles, tiles.y = splits.
+template <int Prec>
+cudaError_t launch_pieces_prec(const GemmArgs& g, void* ws, dim3 tiles, cudaStream_t stream,
+                               int* err_flag, int* kernels) {
+  constexpr int P = Prec == kPrecBF16x6 ? 3 : 2;
+  const int64_t pitch = pieces_pitch(g.K);
+  const int64_t plane_a = 2 * g.M * pitch, plane_b = g.N * pitch;
+  uint16_t* pa = static_cast<uint16_t*>(ws);
+  uint16_t* pb = pa + P * plane_a;
+  TmaMaps maps;
+  if (!make_map_pieces(&maps.a, pa, 2 * g.K, 2 * g.M, pitch, P, 128) ||
+      !make_map_pieces(&maps.b, pb, 2 * g.K, g.N, pitch, P, kTileN / 2))
+    return cudaErrorInvalidConfiguration;
+  const int64_t tiles_k = (g.K + 31) / 32;
+  const int64_t blocks_a = (g.M + 31) / 32 * tiles_k, blocks_b = (g.N + 31) / 32 * tiles_k;
+  if (blocks_a + blocks_b >= (int64_t(1) << 31)) return cudaErrorInvalidConfiguration;
+  split_pieces<P><<<static_cast<unsigned>(blocks_a + blocks_b), 256, 0, stream>>>(
+      g, pa, pb, pitch, plane_a, plane_b, blocks_a, tiles_k);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  ++*kernels;
+  constexpr int kSmem = pc_smem_bytes<P>();
+  static_assert(kSmem <= 227 * 1024, "shared memory budget");
+  static bool attr_set = false;
+  if (!attr_set) {
+    e = cudaFuncSetAttribute(tc1m_pieces<Prec>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = tiles;
+  cfg.blockDim = dim3(kThreads1);
+  cfg.dynamicSmemBytes = kSmem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, tc1m_pieces<Prec>, g, maps, err_flag);
 }
 
 template <int AMode, int Prec, bool kReal>
@@ -2385,6 +2789,14 @@ size_t tc_pack_bytes(int dtype, const HostPlan& plan) {
   return b;
 }
 
+size_t tc_pieces_bytes(int dtype, int method, int64_t M, int64_t N, int64_t K) {
+  if (dtype != T1M_COMPLEX64 || M <= 2 * kTileMc || N <= 0 || K <= 0) return 0;
+  if (method != T1M_METHOD_TC_BF16X3 && method != T1M_METHOD_TC_BF16X6 && method != kMethodTcAuto)
+    return 0;
+  const size_t pieces = method == T1M_METHOD_TC_BF16X3 ? 2 : 3;
+  return pieces * static_cast<size_t>(2 * M + N) * static_cast<size_t>(pieces_pitch(K)) * 2u;
+}
+
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
   const bool real = dtype == T1M_FLOAT32;
   if ((dtype != T1M_COMPLEX64 && !real) || M <= 0 || N <= 0 || K <= 0) return 0;
@@ -2601,12 +3013,22 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                           : make_map(&pmaps.b, p.g.B, p.g.N, p.g.K, packed_plan->uB_k, kTileN,
                                      kStepK, false);
     }
+    // Operand pieces (bf16 methods): the pairs' MMAs read operands split
+    // once beforehand into the panel workspace, for T1M_TILE_PIECES.
+    const bool pieces = pair && bf16 && form == T1M_TILE_PIECES && panel &&
+                        panel_bytes >= tc_pieces_bytes(dtype, method, p.g.M, p.g.N, p.g.K);
     if (pair) {
       const int64_t pair_m = (p.g.M + 2 * kTileMc - 1) / (2 * kTileMc);
       const dim3 pgrid(static_cast<unsigned>(2 * pair_m * p.tiles_n), static_cast<unsigned>(splits));
-      e = launch_pair_prec(method, am, bm, p.g, pmaps, stream, err_flag, pgrid);
+      if (pieces) {
+        e = method == T1M_METHOD_TC_BF16X3
+                ? launch_pieces_prec<kPrecBF16x3>(p.g, panel, pgrid, stream, err_flag, kernels)
+                : launch_pieces_prec<kPrecBF16x6>(p.g, panel, pgrid, stream, err_flag, kernels);
+      } else {
+        e = launch_pair_prec(method, am, bm, p.g, pmaps, stream, err_flag, pgrid);
+      }
       set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A, false);
-      if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR;
+      if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR | (pieces ? T1M_PATH_PIECES : 0);
     } else {
       if (panels)
         if ((e = use_panels(p.g, &maps, &bm)) != cudaSuccess) return e;
