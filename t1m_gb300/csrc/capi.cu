@@ -62,6 +62,10 @@ struct t1m_context {
   size_t panel_bytes[2] = {0, 0};
   void* pack[2] = {nullptr, nullptr};
   size_t pack_bytes[2] = {0, 0};
+  // Host-buffer pipeline: pieces of its resident operand, split once for
+  // every slab (grow only; an optional workspace like the panels).
+  void* res_pieces = nullptr;
+  size_t res_pieces_bytes = 0;
   int split_k = 0;
   // Cap on each optional workspace (panels, packs); -1 = none.
   int64_t opt_work_limit = -1;
@@ -84,7 +88,7 @@ struct t1m_context {
   // between the context stream and this one, so the last wave of one slab's
   // kernel shares the SMs with the first of the next.
   cudaStream_t compute2 = nullptr;
-  static constexpr int kPipeEvents = 3 + 8 + 2 * 8 + 2;
+  static constexpr int kPipeEvents = 3 + 8 + 2 * 8 + 2 + 2;
   cudaEvent_t pev[kPipeEvents] = {};
 };
 
@@ -322,7 +326,8 @@ bool tuned_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
 // kernel launch.  Adds the kernels it launched to *kernels.
 int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const HostPlan& hp,
                    const GemmArgs& g, cudaStream_t s, int* kernels, int* used_method,
-                   int* splits_out, int slot, bool allow_split) {
+                   int* splits_out, int slot, bool allow_split,
+                   const PiecesReady* ready = nullptr) {
   int nk = 0;
   int splits = 1;
   cudaError_t e = cudaSuccess;
@@ -385,10 +390,11 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       const auto within = [&](size_t bytes) {
         return ctx->opt_work_limit < 0 || bytes <= static_cast<size_t>(ctx->opt_work_limit);
       };
-      const size_t pb = std::max(tc_panel_bytes(dtype, gm.M, gm.N, gm.K),
-                                 form == T1M_TILE_PIECES
-                                     ? tc_pieces_bytes(dtype, method, gm.M, gm.N, gm.K)
-                                     : size_t(0));
+      // The panel workspace also holds operand pieces where they run.
+      const size_t pcb = tc_pieces_count(method, dtype, gm, hp, form) > 0
+                             ? tc_pieces_bytes(dtype, method, gm.M, gm.N, gm.K, ready)
+                             : 0;
+      const size_t pb = std::max(tc_panel_bytes(dtype, gm.M, gm.N, gm.K), pcb);
       const bool pan = pb > 0 && within(pb) &&
                        ensure_opt_work(s, &ctx->panel[slot], &ctx->panel_bytes[slot], pb);
       const size_t kb = tc_pack_bytes(dtype, hp);
@@ -397,7 +403,7 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
                     pan ? ctx->panel[slot] : nullptr, pan ? ctx->panel_bytes[slot] : 0,
                     pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0,
-                    &ctx->last_path, form);
+                    &ctx->last_path, form, ready);
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -488,7 +494,8 @@ enum : int {
   kEvDone = kEvSlab + kMaxSlabs,     // + 2 i + h: block (i, h) computed
   kEvOut = kEvDone + 2 * kMaxSlabs,  // copy_out finished
   kEvC2 = kEvOut + 1,                // compute2 finished
-  kEvCount = kEvC2 + 1
+  kEvResPieces = kEvC2 + 1,          // + h: pieces of resident half h split
+  kEvCount = kEvResPieces + 2
 };
 static_assert(kEvCount <= t1m_context::kPipeEvents, "pipeline events");
 
@@ -566,11 +573,7 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   // Block (slab i, half h): the slab dimension shortened to the slab, the
   // halved dimension to the half, operands and C shifted accordingly
   // (uniform strides, so no scatter vector changes).
-  auto launch_block = [&](int i, int h) -> int {
-    const int slot = nblock++ & 1;
-    cudaStream_t cs = slot ? ctx->compute2 : s;
-    cudaStreamWaitEvent(cs, ctx->pev[kEvRes + h], 0);
-    cudaStreamWaitEvent(cs, ctx->pev[kEvSlab + i], 0);
+  auto block_args = [&](int i, int h) -> GemmArgs {
     const int64_t lo = i * sl.width, hi = std::min(len, lo + sl.width);
     const int64_t hlo = split ? h * half : 0, hhi = split ? (h ? rlen : half) : rlen;
     GemmArgs gs = g0;
@@ -598,8 +601,51 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
     }
     gs.k_per_split = hp.K;
     gs.c_split_stride = 0;
+    return gs;
+  };
+  // Operand pieces: where the blocks run as pieces, the resident operand is
+  // split once, half by half after its copy (on the context stream), into
+  // its own workspace; every block then splits only its streamed slab.
+  const int npieces = tc_pieces_count(method, dtype, block_args(0, 0), hp, ctx->tile_form);
+  const int64_t ppitch = tc_pieces_pitch(hp.K);
+  const int64_t prows = sl.along_n ? 2 * hp.M : hp.N;   // rows of the resident pieces
+  const size_t pbytes = size_t(npieces) * size_t(prows) * size_t(ppitch) * 2u;
+  const bool res_pieces =
+      npieces > 0 && (ctx->opt_work_limit < 0 || pbytes <= size_t(ctx->opt_work_limit)) &&
+      ensure_opt_work(s, &ctx->res_pieces, &ctx->res_pieces_bytes, pbytes);
+  // Element offset of half h's first row in the resident pieces.
+  auto pieces_row0 = [&](int h) -> int64_t {
+    const int64_t hlo = split ? h * half : 0;
+    return (sl.along_n ? 2 * hlo : hlo) * ppitch;
+  };
+  auto split_resident = [&](int h) -> cudaError_t {
+    cudaStreamWaitEvent(s, ctx->pev[kEvRes + h], 0);
+    void* out = static_cast<uint16_t*>(ctx->res_pieces) + pieces_row0(h);
+    const cudaError_t r =
+        tc_split_operand(npieces, sl.along_n, block_args(0, h), out, prows * ppitch, s);
+    if (r == cudaSuccess) ++kernels;
+    cudaEventRecord(ctx->pev[kEvResPieces + h], s);
+    return r;
+  };
+  auto launch_block = [&](int i, int h) -> int {
+    const int slot = nblock++ & 1;
+    cudaStream_t cs = slot ? ctx->compute2 : s;
+    cudaStreamWaitEvent(cs, ctx->pev[res_pieces ? kEvResPieces + h : kEvRes + h], 0);
+    cudaStreamWaitEvent(cs, ctx->pev[kEvSlab + i], 0);
+    const GemmArgs gs = block_args(i, h);
+    PiecesReady ready;
+    if (res_pieces) {
+      const void* p = static_cast<const uint16_t*>(ctx->res_pieces) + pieces_row0(h);
+      if (sl.along_n) {
+        ready.a = p;
+        ready.a_plane = prows * ppitch;
+      } else {
+        ready.b = p;
+        ready.b_plane = prows * ppitch;
+      }
+    }
     if (int st = launch_product(ctx, method, dtype, es, hp, gs, cs, &kernels, &used_method,
-                                &splits, slot, false))
+                                &splits, slot, false, res_pieces ? &ready : nullptr))
       return st;
     cudaEventRecord(ctx->pev[kEvDone + 2 * i + h], cs);
     return T1M_OK;
@@ -618,6 +664,8 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   // Copies in order, each followed by the blocks it completes.
   if ((e = copy_resident(0)) != cudaSuccess) return cuda_fail(ctx, e, "copy resident operand");
   cudaEventRecord(ctx->pev[kEvRes], ctx->copy_in);
+  if (res_pieces && (e = split_resident(0)) != cudaSuccess)
+    return cuda_fail(ctx, e, "split resident operand");
   const int early = split ? std::min(2, sl.count) : 0;  // slabs before the second half
   for (int i = 0; i < early; ++i) {
     if ((e = copy_slab(i)) != cudaSuccess) return cuda_fail(ctx, e, "copy slab to device");
@@ -626,6 +674,8 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   if (split) {
     if ((e = copy_resident(1)) != cudaSuccess) return cuda_fail(ctx, e, "copy resident operand");
     cudaEventRecord(ctx->pev[kEvRes + 1], ctx->copy_in);
+    if (res_pieces && (e = split_resident(1)) != cudaSuccess)
+      return cuda_fail(ctx, e, "split resident operand");
     for (int i = 0; i < early; ++i) {
       if (int st = launch_block(i, 1)) return st;
       if ((e = copy_back(i)) != cudaSuccess) return cuda_fail(ctx, e, "copy C slab to host");
@@ -779,6 +829,7 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->panel[i]) cudaFree(ctx->panel[i]);
     if (ctx->pack[i]) cudaFree(ctx->pack[i]);
   }
+  if (ctx->res_pieces) cudaFree(ctx->res_pieces);
   if (ctx->compute2) {
     cudaStreamSynchronize(ctx->compute2);
     cudaStreamDestroy(ctx->compute2);
@@ -1276,7 +1327,9 @@ bool tuned_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
     code = it->second;
   } else {
     float best = 1e30f;
-    for (int f : {T1M_TILE_ONE, T1M_TILE_PAIR}) {
+    for (int f : {T1M_TILE_ONE, T1M_TILE_PAIR, T1M_TILE_PIECES}) {
+      // Pieces only where they run (else the same as pairs).
+      if (f == T1M_TILE_PIECES && tc_pieces_count(method, dtype, g, hp, f) == 0) continue;
       int last_sp = -1;
       for (int v = 0; v < 3; ++v) {
         const int sp = variant(v);
@@ -1302,7 +1355,7 @@ bool tuned_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
         GemmArgs red = gm;
         red.C = work + size_t(sp) * size_t(g.M) * size_t(g.N) * es;
         const size_t pb = std::max(tc_panel_bytes(dtype, gm.M, gm.N, gm.K),
-                                   f == T1M_TILE_PIECES
+                                   tc_pieces_count(method, dtype, gm, hp, f) > 0
                                        ? tc_pieces_bytes(dtype, method, gm.M, gm.N, gm.K)
                                        : size_t(0));
         const bool pan = pb > 0 && (ctx->opt_work_limit < 0 || pb <= size_t(ctx->opt_work_limit)) &&

@@ -197,6 +197,18 @@ struct SplitReduce {
 cudaError_t launch_splitk_reduce_group(int dtype, const SplitReduce* dev, int n,
                                        int64_t total, cudaStream_t stream);
 
+// Operand pieces already in device memory (the host-buffer pipeline splits
+// its resident operand once for all slabs): P bf16 arrays per operand, rows
+// tc_pieces_pitch(K) elements apart, `*_plane` elements between arrays; A's
+// rows are the 1M rows (two per complex row), B's one per column.  Null
+// pointers: the product splits that operand itself.
+struct PiecesReady {
+  const void* a = nullptr;
+  int64_t a_plane = 0;
+  const void* b = nullptr;
+  int64_t b_plane = 0;
+};
+
 // tc.cu: one contraction on the tensor cores (complex64 / float32, split
 // methods).  `panel` (panel_bytes) is workspace for B split once into
 // panels, at least tc_panel_bytes(dtype, M, N, K) bytes, or null.
@@ -207,13 +219,23 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel = nullptr,
                       size_t panel_bytes = 0, void* pack = nullptr, size_t pack_bytes = 0,
-                      int* path = nullptr, int form = 0 /* T1M_TILE_* */);
+                      int* path = nullptr, int form = 0 /* T1M_TILE_* */,
+                      const PiecesReady* ready = nullptr);
 // Panel workspace a product would use (0: panels not used at this size).
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K);
 // Bytes of the operand pieces of the T1M_TILE_PIECES form (held in the panel
 // workspace), 0 where that form does not apply.  kMethodTcAuto counts the
-// BF16x6 pieces.
-size_t tc_pieces_bytes(int dtype, int method, int64_t M, int64_t N, int64_t K);
+// BF16x6 pieces.  With `ready`, only the operands it does not hold.
+size_t tc_pieces_bytes(int dtype, int method, int64_t M, int64_t N, int64_t K,
+                       const PiecesReady* ready = nullptr);
+int64_t tc_pieces_pitch(int64_t K);
+// Pieces per element (2 or 3) the product would be split into by launch_tc
+// with this method and tile form, 0 if it would not run as pieces.
+int tc_pieces_count(int method, int dtype, const GemmArgs& g, const HostPlan& plan, int form);
+// Split operand A (the 1M rows of its M rows) or B (its N rows) of g into
+// `pieces` arrays at `out`, `plane` elements apart (one launch on s).
+cudaError_t tc_split_operand(int pieces, bool operand_a, const GemmArgs& g, void* out,
+                             int64_t plane, cudaStream_t s);
 // Pack workspace a product may use (0: neither operand would be packed).
 size_t tc_pack_bytes(int dtype, const HostPlan& plan);
 

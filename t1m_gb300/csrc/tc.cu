@@ -2301,10 +2301,11 @@ cudaError_t launch_pair_prec(int method, int amode, int bmode, const GemmArgs& a
 // Operand pieces: row pitch in bf16 elements (real K rounded up to 16 bytes).
 int64_t pieces_pitch(int64_t K) { return (2 * K + 7) / 8 * 8; }
 
-// 3-D map over P piece arrays of `rows` rows of `kreal` bf16 (`pitch`
-// apart), loaded as boxes of 64 k x box_rows x P with the 128-byte swizzle.
+// 3-D map over P piece arrays (`plane` elements apart) of `rows` rows of
+// `kreal` bf16 (`pitch` apart), loaded as boxes of 64 k x box_rows x P with
+// the 128-byte swizzle.
 bool make_map_pieces(CUtensorMap* map, const void* base, int64_t kreal, int64_t rows,
-                     int64_t pitch, int pieces, uint32_t box_rows) {
+                     int64_t pitch, int64_t plane, int pieces, uint32_t box_rows) {
   EncodeTiledFn fn = encode_fn();
   if (!fn || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
   if (kreal <= 0 || rows <= 0 || kreal >= (int64_t(1) << 31) || rows >= (int64_t(1) << 31))
@@ -2312,7 +2313,7 @@ bool make_map_pieces(CUtensorMap* map, const void* base, int64_t kreal, int64_t 
   cuuint64_t dims[3] = {static_cast<cuuint64_t>(kreal), static_cast<cuuint64_t>(rows),
                         static_cast<cuuint64_t>(pieces)};
   cuuint64_t strides[2] = {static_cast<cuuint64_t>(pitch * 2),
-                           static_cast<cuuint64_t>(rows * pitch * 2)};
+                           static_cast<cuuint64_t>(plane * 2)};
   cuuint32_t box[3] = {static_cast<cuuint32_t>(kPcStepK), box_rows, static_cast<cuuint32_t>(pieces)};
   cuuint32_t estr[3] = {1, 1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 3, const_cast<void*>(base), dims, strides, box,
@@ -2320,28 +2321,35 @@ bool make_map_pieces(CUtensorMap* map, const void* base, int64_t kreal, int64_t 
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// The pieces of A and B (one launch, counted in *kernels), then the pair
-// kernel over them: tiles.x = 2 x pair tiles, tiles.y = splits.
+// The pieces of A and B not in `ready` (one launch, counted in *kernels;
+// into ws, A's first), then the pair kernel over them: tiles.x = 2 x pair
+// tiles, tiles.y = splits.
 template <int Prec>
-cudaError_t launch_pieces_prec(const GemmArgs& g, void* ws, dim3 tiles, cudaStream_t stream,
-                               int* err_flag, int* kernels) {
+cudaError_t launch_pieces_prec(const GemmArgs& g, void* ws, const PiecesReady* ready, dim3 tiles,
+                               cudaStream_t stream, int* err_flag, int* kernels) {
   constexpr int P = Prec == kPrecBF16x6 ? 3 : 2;
   const int64_t pitch = pieces_pitch(g.K);
-  const int64_t plane_a = 2 * g.M * pitch, plane_b = g.N * pitch;
-  uint16_t* pa = static_cast<uint16_t*>(ws);
-  uint16_t* pb = pa + P * plane_a;
+  const bool ra = ready && ready->a, rb = ready && ready->b;
+  const int64_t plane_a = ra ? ready->a_plane : 2 * g.M * pitch;
+  const int64_t plane_b = rb ? ready->b_plane : g.N * pitch;
+  uint16_t* const w = static_cast<uint16_t*>(ws);
+  uint16_t* pa = ra ? static_cast<uint16_t*>(const_cast<void*>(ready->a)) : w;
+  uint16_t* pb = rb ? static_cast<uint16_t*>(const_cast<void*>(ready->b)) : w + (ra ? 0 : P * plane_a);
   TmaMaps maps;
-  if (!make_map_pieces(&maps.a, pa, 2 * g.K, 2 * g.M, pitch, P, 128) ||
-      !make_map_pieces(&maps.b, pb, 2 * g.K, g.N, pitch, P, kTileN / 2))
+  if (!make_map_pieces(&maps.a, pa, 2 * g.K, 2 * g.M, pitch, plane_a, P, 128) ||
+      !make_map_pieces(&maps.b, pb, 2 * g.K, g.N, pitch, plane_b, P, kTileN / 2))
     return cudaErrorInvalidConfiguration;
   const int64_t tiles_k = (g.K + 31) / 32;
-  const int64_t blocks_a = (g.M + 31) / 32 * tiles_k, blocks_b = (g.N + 31) / 32 * tiles_k;
+  const int64_t blocks_a = ra ? 0 : (g.M + 31) / 32 * tiles_k;
+  const int64_t blocks_b = rb ? 0 : (g.N + 31) / 32 * tiles_k;
   if (blocks_a + blocks_b >= (int64_t(1) << 31)) return cudaErrorInvalidConfiguration;
-  split_pieces<P><<<static_cast<unsigned>(blocks_a + blocks_b), 256, 0, stream>>>(
-      g, pa, pb, pitch, plane_a, plane_b, blocks_a, tiles_k);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  ++*kernels;
+  cudaError_t e;
+  if (blocks_a + blocks_b > 0) {
+    split_pieces<P><<<static_cast<unsigned>(blocks_a + blocks_b), 256, 0, stream>>>(
+        g, pa, pb, pitch, plane_a, plane_b, blocks_a, tiles_k);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    ++*kernels;
+  }
   constexpr int kSmem = pc_smem_bytes<P>();
   static_assert(kSmem <= 227 * 1024, "shared memory budget");
   static bool attr_set = false;
@@ -2789,12 +2797,34 @@ size_t tc_pack_bytes(int dtype, const HostPlan& plan) {
   return b;
 }
 
-size_t tc_pieces_bytes(int dtype, int method, int64_t M, int64_t N, int64_t K) {
-  if (dtype != T1M_COMPLEX64 || M <= 2 * kTileMc || N <= 0 || K <= 0) return 0;
+size_t tc_pieces_bytes(int dtype, int method, int64_t M, int64_t N, int64_t K,
+                       const PiecesReady* ready) {
+  if (dtype != T1M_COMPLEX64 || M <= kTileMc || N <= 0 || K <= 0) return 0;
   if (method != T1M_METHOD_TC_BF16X3 && method != T1M_METHOD_TC_BF16X6 && method != kMethodTcAuto)
     return 0;
   const size_t pieces = method == T1M_METHOD_TC_BF16X3 ? 2 : 3;
-  return pieces * static_cast<size_t>(2 * M + N) * static_cast<size_t>(pieces_pitch(K)) * 2u;
+  const int64_t rows = (ready && ready->a ? 0 : 2 * M) + (ready && ready->b ? 0 : N);
+  return pieces * static_cast<size_t>(rows) * static_cast<size_t>(pieces_pitch(K)) * 2u;
+}
+
+int64_t tc_pieces_pitch(int64_t K) { return pieces_pitch(K); }
+
+cudaError_t tc_split_operand(int pieces, bool operand_a, const GemmArgs& g, void* out,
+                             int64_t plane, cudaStream_t s) {
+  const int64_t pitch = pieces_pitch(g.K);
+  const int64_t tiles_k = (g.K + 31) / 32;
+  const int64_t blocks = ((operand_a ? g.M : g.N) + 31) / 32 * tiles_k;
+  if (blocks <= 0) return cudaSuccess;
+  if (blocks >= (int64_t(1) << 31)) return cudaErrorInvalidConfiguration;
+  uint16_t* o = static_cast<uint16_t*>(out);
+  const unsigned grid = static_cast<unsigned>(blocks);
+  // B alone: no A blocks (blocks_a = 0), B's arrays at o.
+  const int64_t ba = operand_a ? blocks : 0;
+  if (pieces == 2)
+    split_pieces<2><<<grid, 256, 0, s>>>(g, o, o, pitch, plane, plane, ba, tiles_k);
+  else
+    split_pieces<3><<<grid, 256, 0, s>>>(g, o, o, pitch, plane, plane, ba, tiles_k);
+  return cudaGetLastError();
 }
 
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
@@ -2805,10 +2835,37 @@ size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K) {
   return static_cast<size_t>(N) * static_cast<size_t>(panel_stages(real, K)) * 256u;
 }
 
+// Method of the pieces form for a product, 0 where it does not run: the
+// bf16 methods (the automatic method as BF16x6) with two or more 64-row M
+// tiles; any operand layout for T1M_TILE_PIECES (the split pass reads through
+// the scatter vectors), for T1M_TILE_AUTO where both operands load by TMA
+// (where CTA pairs would otherwise run).
+static int pieces_method(int method, int form, const TcProblem& p) {
+  if (p.tiles_m < 2) return 0;
+  const int pm = method == kMethodTcAuto ? T1M_METHOD_TC_BF16X6 : method;
+  if (pm != T1M_METHOD_TC_BF16X3 && pm != T1M_METHOD_TC_BF16X6) return 0;
+  if (form == T1M_TILE_PIECES) return pm;
+  if (form != T1M_TILE_AUTO) return 0;
+  const bool a_block = (p.block_maps & 1) || p.amode == kAMK16;
+  const bool b_block = (p.block_maps & 2) != 0;
+  const bool tma_a = !a_block && (p.amode == kAMK || p.amode == kAKM);
+  const bool tma_b = !b_block && (p.bmode == kBNK || p.bmode == kBKN);
+  return tma_a && tma_b ? pm : 0;
+}
+
+int tc_pieces_count(int method, int dtype, const GemmArgs& g, const HostPlan& plan, int form) {
+  if (dtype != T1M_COMPLEX64 || !tc_supported(method, dtype, plan)) return 0;
+  TcProblem p;
+  if (!tc_prepare(g, plan, 1, &p)) return 0;
+  const int pm = pieces_method(method, form, p);
+  return pm == T1M_METHOD_TC_BF16X3 ? 2 : pm == T1M_METHOD_TC_BF16X6 ? 3 : 0;
+}
+
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel, size_t panel_bytes,
-                      void* pack, size_t pack_bytes, int* path, int form) {
+                      void* pack, size_t pack_bytes, int* path, int form,
+                      const PiecesReady* ready) {
   *kernels = 0;
   if (used_method) *used_method = method;
   if (path) *path = 0;
@@ -2950,6 +3007,26 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
   }
   TcProblem p;
   if (!tc_prepare(args, plan, splits, &p)) return cudaErrorInvalidConfiguration;
+  if (const int pm = pieces_method(method, form, p)) {
+    // Operand pieces: split once (the operands not in `ready`) into the
+    // panel workspace, then CTA pairs with both MMA operands in shared
+    // memory.  Without the workspace the product takes the forms below.
+    const size_t need = tc_pieces_bytes(dtype, pm, args.M, args.N, args.K, ready);
+    if (need == 0 || (panel && panel_bytes >= need)) {
+      if (used_method) *used_method = pm;
+      const int64_t pair_m = (p.g.M + 2 * kTileMc - 1) / (2 * kTileMc);
+      const dim3 pgrid(static_cast<unsigned>(2 * pair_m * p.tiles_n),
+                       static_cast<unsigned>(splits));
+      const cudaError_t e =
+          pm == T1M_METHOD_TC_BF16X3
+              ? launch_pieces_prec<kPrecBF16x3>(p.g, panel, ready, pgrid, stream, err_flag, kernels)
+              : launch_pieces_prec<kPrecBF16x6>(p.g, panel, ready, pgrid, stream, err_flag, kernels);
+      if (e == cudaSuccess) ++*kernels;
+      set_path(p.amode, p.bmode, false, false, false);
+      if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR | T1M_PATH_PIECES;
+      return e;
+    }
+  }
   {
     // A per-16-row block-TMA operand A is packed as well when that puts the
     // product on the one-tile kernel (B by TMA or by panels): the block form
@@ -3013,22 +3090,12 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                           : make_map(&pmaps.b, p.g.B, p.g.N, p.g.K, packed_plan->uB_k, kTileN,
                                      kStepK, false);
     }
-    // Operand pieces (bf16 methods): the pairs' MMAs read operands split
-    // once beforehand into the panel workspace, for T1M_TILE_PIECES.
-    const bool pieces = pair && bf16 && form == T1M_TILE_PIECES && panel &&
-                        panel_bytes >= tc_pieces_bytes(dtype, method, p.g.M, p.g.N, p.g.K);
     if (pair) {
       const int64_t pair_m = (p.g.M + 2 * kTileMc - 1) / (2 * kTileMc);
       const dim3 pgrid(static_cast<unsigned>(2 * pair_m * p.tiles_n), static_cast<unsigned>(splits));
-      if (pieces) {
-        e = method == T1M_METHOD_TC_BF16X3
-                ? launch_pieces_prec<kPrecBF16x3>(p.g, panel, pgrid, stream, err_flag, kernels)
-                : launch_pieces_prec<kPrecBF16x6>(p.g, panel, pgrid, stream, err_flag, kernels);
-      } else {
-        e = launch_pair_prec(method, am, bm, p.g, pmaps, stream, err_flag, pgrid);
-      }
+      e = launch_pair_prec(method, am, bm, p.g, pmaps, stream, err_flag, pgrid);
       set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A, false);
-      if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR | (pieces ? T1M_PATH_PIECES : 0);
+      if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR;
     } else {
       if (panels)
         if ((e = use_panels(p.g, &maps, &bm)) != cudaSuccess) return e;

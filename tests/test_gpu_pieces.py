@@ -146,3 +146,41 @@ def test_pieces_without_workspace(ctx, torch_cuda):
         ctx.set_workspace_limit(-1)
     assert rq.fetch["pair"] and not rq.fetch["pieces"]
     assert np.array_equal(pair.view(np.uint64), pieces.view(np.uint64))
+
+
+@pytest.mark.parametrize("layout", ["col", "row"])
+def test_pieces_host_pipeline(ctx, torch_cuda, layout):
+    """Host operands (slab pipeline, slabs along N for col-major and along M
+    for row-major): the resident operand is split into pieces once, each
+    block splits only its streamed slab.  Equal to the device-buffer result
+    and to the pair form's, bit for bit."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    dims = [48] * 4
+    n = 48 ** 4
+    rng = np.random.default_rng(55)
+    A, B = _rand(rng, n), _rand(rng, n)
+    L = t1m.col_major if layout == "col" else t1m.row_major
+    out = {}
+    ctx.set_method("tc_bf16x6")
+    try:
+        for form in ("pieces", "pair"):
+            ctx.set_tile_form(form)
+            ch = np.zeros(n, np.complex64)
+            rep = t1m.contract_scaled(1.0, t1m.tensor(dims, A, L), "ijkl", t1m.tensor(dims, B, L),
+                                      "klmn", 0.0, t1m.tensor(dims, ch, L), "ijmn", ctx=ctx)
+            out[form] = (ch, rep)
+        ctx.set_tile_form("pieces")
+        ga, gb = torch.from_numpy(A).cuda(), torch.from_numpy(B).cuda()
+        gc = torch.zeros(n, dtype=torch.complex64, device="cuda")
+        dev = t1m.contract_scaled(1.0, t1m.tensor(dims, ga, L), "ijkl", t1m.tensor(dims, gb, L),
+                                  "klmn", 0.0, t1m.tensor(dims, gc, L), "ijmn", ctx=ctx)
+        torch.cuda.synchronize()
+    finally:
+        ctx.set_tile_form("auto")
+        ctx.set_method("auto")
+    ch, rep = out["pieces"]
+    assert rep.h2d_bytes >= 2 * n * 8 and rep.fetch["pieces"] and dev.fetch["pieces"]
+    assert not out["pair"][1].fetch["pieces"]
+    np.testing.assert_array_equal(ch, gc.cpu().numpy())
+    np.testing.assert_array_equal(ch, out["pair"][0])

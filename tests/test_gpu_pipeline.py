@@ -12,12 +12,13 @@ def _rand(rng, n, dt):
     return (rng.uniform(-1, 1, n) + 1j * rng.uniform(-1, 1, n)).astype(dt)
 
 
-@pytest.mark.parametrize("method", ["tc_3xtf32", "plain"])
+@pytest.mark.parametrize("method", ["tc_3xtf32", "tc_bf16x6", "plain"])
 @pytest.mark.parametrize("layout", ["col", "row"])
 @pytest.mark.parametrize("beta", [0.0, 0.25])
 def test_pipelined_host_equals_device(ctx, torch_cuda, layout, method, beta):
     """ijkl,klmn->ijmn, extents 48 (A, B, C 42 MB each): slabs along N for
-    col-major, along M for row-major; beta != 0 also streams C in."""
+    col-major, along M for row-major; beta != 0 also streams C in.  BF16x6
+    runs as operand pieces: the resident operand split once for all slabs."""
     import t1m_gb300 as t1m
     torch = torch_cuda
     dims = [48] * 4
@@ -40,6 +41,8 @@ def test_pipelined_host_equals_device(ctx, torch_cuda, layout, method, beta):
         ctx.set_method("auto")
     assert rep.kernels >= 2  # one product per slab
     assert rep.h2d_bytes >= 2 * n * 8 and rep.d2h_bytes == n * 8
+    if method == "tc_bf16x6":
+        assert rep.fetch["pieces"], rep.fetch
     np.testing.assert_array_equal(ch, gc.cpu().numpy())
 
 
