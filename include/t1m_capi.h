@@ -96,6 +96,10 @@ typedef struct t1m_report {
   int32_t path;        /* tensor-core products: T1M_PATH_* code of the last
                           product (how its operands were fetched); 0 for
                           the plain and FP64 kernels                         */
+  double main_ms;      /* device time of the last tensor-core product's main
+                          kernel alone (without its split, pack, panel and
+                          split-K reduction passes); timed single calls with
+                          device operands only, else 0                       */
 } t1m_report;
 
 /* t1m_report.path: bit 12 marks a tensor-core product; bits 0-3 the fetch

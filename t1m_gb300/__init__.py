@@ -93,7 +93,7 @@ class Report(C.Structure):
                 ("n", C.c_int64), ("k", C.c_int64), ("flops", C.c_double),
                 ("kernel_ms", C.c_double), ("h2d_ms", C.c_double), ("d2h_ms", C.c_double),
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64), ("kernels", C.c_int32),
-                ("path", C.c_int32)]
+                ("path", C.c_int32), ("main_ms", C.c_double)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

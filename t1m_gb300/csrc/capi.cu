@@ -40,6 +40,11 @@ struct t1m_context {
   int method = T1M_METHOD_AUTO;
   std::string last_error;
   cudaEvent_t ev[6] = {};
+  // Around the main kernel of a tensor-core product (after its split, pack
+  // or panel passes), when a timed single-product call arms them.
+  cudaEvent_t mev[2] = {};
+  bool mev_armed = false;
+  bool mev_recorded = false;
   // Device-side error word written by kernels whose bounded waits ran out.
   int* d_err = nullptr;
   // Plan cache: key -> (host plan, device scatter vectors), LRU bounded.
@@ -403,7 +408,8 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
                     pan ? ctx->panel[slot] : nullptr, pan ? ctx->panel_bytes[slot] : 0,
                     pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0,
-                    &ctx->last_path, form, ready);
+                    &ctx->last_path, form, ready, ctx->mev_armed ? ctx->mev : nullptr);
+      if (e == cudaSuccess && ctx->mev_armed) ctx->mev_recorded = true;
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
@@ -764,6 +770,7 @@ int t1m_create(t1m_context** out, int device) {
   cudaError_t e = cudaSetDevice(device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking);
   for (int i = 0; i < 6 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->ev[i]);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) e = cudaEventCreate(&ctx->mev[i]);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_in, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_out, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->compute2, cudaStreamNonBlocking);
@@ -823,6 +830,8 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->stage[i]) cudaFree(ctx->stage[i]);
   for (int i = 0; i < 6; ++i)
     if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+  for (int i = 0; i < 2; ++i)
+    if (ctx->mev[i]) cudaEventDestroy(ctx->mev[i]);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->work) cudaFree(ctx->work);
   for (int i = 0; i < 2; ++i) {
@@ -1051,6 +1060,8 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     g.C = ctx->stage[2];
   }
   if (timing) cudaEventRecord(ctx->ev[1], s);
+  ctx->mev_armed = timing;
+  ctx->mev_recorded = false;
 
   int kernels = 0;
   int used_method = method;
@@ -1067,10 +1078,14 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
     g.C = static_cast<char*>(g_all.C) + oc * static_cast<int64_t>(es);
     g.k_per_split = std::max<int64_t>(hp.K, 1);
     g.c_split_stride = 0;
-    if (int st = launch_product(ctx, method, dtype, es, hp, g, s, &kernels, &used_method, &splits,
-                                0, true))
+    const int st = launch_product(ctx, method, dtype, es, hp, g, s, &kernels, &used_method,
+                                  &splits, 0, true);
+    if (st) {
+      ctx->mev_armed = false;
       return st;
+    }
   }
+  ctx->mev_armed = false;
   if (timing) cudaEventRecord(ctx->ev[2], s);
   if (!devC && bytesC) {
     if ((e = cudaMemcpyAsync(c->data, ctx->stage[2], bytesC, cudaMemcpyDeviceToHost, s)) != cudaSuccess)
@@ -1105,6 +1120,9 @@ int t1m_contract(t1m_context* ctx, int dtype, const void* alpha, const t1m_tenso
       report->h2d_ms = t01;
       report->kernel_ms = t12;
       report->d2h_ms = t23;
+      float tm = 0;
+      if (ctx->mev_recorded && cudaEventElapsedTime(&tm, ctx->mev[0], ctx->mev[1]) == cudaSuccess)
+        report->main_ms = tm;
     }
   }
   return T1M_OK;

@@ -2326,7 +2326,8 @@ bool make_map_pieces(CUtensorMap* map, const void* base, int64_t kreal, int64_t 
 // tiles, tiles.y = splits.
 template <int Prec>
 cudaError_t launch_pieces_prec(const GemmArgs& g, void* ws, const PiecesReady* ready, dim3 tiles,
-                               cudaStream_t stream, int* err_flag, int* kernels) {
+                               cudaStream_t stream, int* err_flag, int* kernels,
+                               cudaEvent_t* main_ev) {
   constexpr int P = Prec == kPrecBF16x6 ? 3 : 2;
   const int64_t pitch = pieces_pitch(g.K);
   const bool ra = ready && ready->a, rb = ready && ready->b;
@@ -2370,7 +2371,10 @@ cudaError_t launch_pieces_prec(const GemmArgs& g, void* ws, const PiecesReady* r
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, tc1m_pieces<Prec>, g, maps, err_flag);
+  if (main_ev) cudaEventRecord(main_ev[0], stream);
+  e = cudaLaunchKernelEx(&cfg, tc1m_pieces<Prec>, g, maps, err_flag);
+  if (main_ev) cudaEventRecord(main_ev[1], stream);
+  return e;
 }
 
 template <int AMode, int Prec, bool kReal>
@@ -2865,8 +2869,11 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel, size_t panel_bytes,
                       void* pack, size_t pack_bytes, int* path, int form,
-                      const PiecesReady* ready) {
+                      const PiecesReady* ready, cudaEvent_t* main_ev) {
   *kernels = 0;
+  auto mark = [&](int i) {
+    if (main_ev) cudaEventRecord(main_ev[i], stream);
+  };
   if (used_method) *used_method = method;
   if (path) *path = 0;
   // The report's path code: fetch modes in TcProblem's numbering, B panels
@@ -2999,7 +3006,9 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
       if (const cudaError_t e = use_panels(gr, &maps, &bm)) return e;
     const dim3 grid(static_cast<unsigned>(((args.M + 127) / 128) * ((args.N + kTileN - 1) / kTileN)),
                     static_cast<unsigned>(splits));
+    mark(0);
     const cudaError_t e = launch_prec<true>(method, am, bm, gr, maps, stream, err_flag, grid);
+    mark(1);
     if (e == cudaSuccess) ++*kernels;
     set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A,
              packed_args.B != args.B);
@@ -3019,8 +3028,10 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                        static_cast<unsigned>(splits));
       const cudaError_t e =
           pm == T1M_METHOD_TC_BF16X3
-              ? launch_pieces_prec<kPrecBF16x3>(p.g, panel, ready, pgrid, stream, err_flag, kernels)
-              : launch_pieces_prec<kPrecBF16x6>(p.g, panel, ready, pgrid, stream, err_flag, kernels);
+              ? launch_pieces_prec<kPrecBF16x3>(p.g, panel, ready, pgrid, stream, err_flag, kernels,
+                                                main_ev)
+              : launch_pieces_prec<kPrecBF16x6>(p.g, panel, ready, pgrid, stream, err_flag, kernels,
+                                                main_ev);
       if (e == cudaSuccess) ++*kernels;
       set_path(p.amode, p.bmode, false, false, false);
       if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR | T1M_PATH_PIECES;
@@ -3093,18 +3104,24 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     if (pair) {
       const int64_t pair_m = (p.g.M + 2 * kTileMc - 1) / (2 * kTileMc);
       const dim3 pgrid(static_cast<unsigned>(2 * pair_m * p.tiles_n), static_cast<unsigned>(splits));
+      mark(0);
       e = launch_pair_prec(method, am, bm, p.g, pmaps, stream, err_flag, pgrid);
+      mark(1);
       set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A, false);
       if (path && e == cudaSuccess) *path |= T1M_PATH_PAIR;
     } else {
       if (panels)
         if ((e = use_panels(p.g, &maps, &bm)) != cudaSuccess) return e;
+      mark(0);
       e = launch_prec<false>(method, am, bm, p.g, maps, stream, err_flag, grid);
+      mark(1);
       set_path(one_tile_a(am), one_tile_b(bm), false, packed_args.A != args.A,
                packed_args.B != args.B);
     }
   } else {
+    mark(0);
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
+    mark(1);
     set_path(p.amode, p.bmode, true, packed_args.A != args.A, packed_args.B != args.B);
   }
   if (e == cudaSuccess) ++*kernels;
