@@ -641,6 +641,16 @@ def workload_batch(args):
         flops += 8.0 * x * y * s * b * a + 8.0 * x * s * t * y * b
     grp = t1m.Group(items, ctx=ctx, graph=True, autotune=not args.no_autotune)
     grouped_ms = _events_ms(torch, lambda: grp.launch(timed=False), args.steps, args.warmup)
+    grouped_kernels = grp.launch().kernels
+    # The same batch as ONE persistent launch (SIMT tiles for the second
+    # steps, split-K reduced in the kernel), for comparison.
+    one = t1m.Group(items, ctx=ctx, graph=True, autotune=not args.no_autotune,
+                    options=t1m.GROUP_ONE_LAUNCH)
+    one_ms = _events_ms(torch, lambda: one.launch(timed=False), args.steps, args.warmup)
+    one_kernels = one.launch().kernels
+    one.close()
+    grp.launch(timed=False)  # outputs of the one-launch form for the check below
+    torch.cuda.synchronize()
     # Sampled check of a few items against FP64.
     errs = []
     for X1, X2, X3, R, O in keep[:4]:
@@ -657,7 +667,11 @@ def workload_batch(args):
     ctx.close()
     print(json.dumps({"workload": f"config4 batch of {n_items} sweep updates (2 contractions each)",
                       "flops_per_batch": flops, "grouped_graph_ms": grouped_ms,
-                      "grouped_tflops": flops / grouped_ms / 1e9, "one_call_at_a_time_ms": single_ms,
+                      "grouped_tflops": flops / grouped_ms / 1e9,
+                      "grouped_kernels": grouped_kernels,
+                      "one_launch_graph_ms": one_ms, "one_launch_kernels": one_kernels,
+                      "one_launch_tflops": flops / one_ms / 1e9,
+                      "one_call_at_a_time_ms": single_ms,
                       "one_call_tflops": flops / single_ms / 1e9,
                       "speedup_grouped": single_ms / grouped_ms, "rel_err_max_sampled": max(errs)}),
           flush=True)

@@ -224,14 +224,25 @@ int t1m_contract_vjp(t1m_context* ctx, int dtype, const t1m_tensor* dc,
  * updates of a tensor-network sweep) run as grouped launches instead of one
  * launch per call.  The reference has no batching (its counterpart is a loop
  * of t1m::contract calls, t1m.h:560-577).  All tensors are device pointers.
- * An item may read the C of an EARLIER item (depends_on = its index); every
- * complex64 item with at least 32 rows and columns runs on the persistent
- * tensor-core kernel, the rest on the grouped plain kernel (a skinny tile for
- * outputs with at most 16 columns).  With T1M_GROUP_AUTOTUNE the family of
- * each shape class (log2 buckets of M, N, K) is measured once and cached in a
- * versioned file ($T1M_TUNE_CACHE, default $HOME/.cache/t1m_gb300_tune.txt,
- * keyed by GPU name, SM count and driver).  With T1M_GROUP_GRAPH the launches
- * are captured once into a CUDA graph that t1m_group_launch replays. */
+ * An item may read the C of an EARLIER item (depends_on = its index).
+ * By default items run per dependency level as one launch per family
+ * (tensor cores for complex64 items with at least 32 rows and columns, the
+ * grouped plain kernel otherwise, a skinny tile for outputs with at most 16
+ * columns) and one split-K reduction; when every item is a tensor-core item
+ * the batch is one persistent launch with the dependencies resolved in the
+ * kernel.  With T1M_GROUP_ONE_LAUNCH a complex64 batch (context method other
+ * than PLAIN) is always ONE persistent launch of the tensor-core kernel:
+ * every item with its own tile (16, 32, 64 or 128 output columns on the
+ * tensor cores, or a SIMT tile for outputs of at most 8 columns),
+ * dependencies resolved in the kernel (a tile of a dependent item waits for
+ * every output tile of its dependency), and items with a long K split
+ * across CTAs and reduced in the kernel (FP64 sum and epilogue by the split
+ * that finishes last).  With T1M_GROUP_AUTOTUNE the family (per-family
+ * launches) or the tile (one launch) of each shape class (log2 buckets of M,
+ * N, K) is measured once and cached in a versioned file ($T1M_TUNE_CACHE,
+ * default $HOME/.cache/t1m_gb300_tune.txt, keyed by GPU name, SM count and
+ * driver).  With T1M_GROUP_GRAPH the launches are captured once into a CUDA
+ * graph that t1m_group_launch replays. */
 typedef struct t1m_group_item {
   const t1m_tensor* a;
   const char* labels_a;
@@ -257,6 +268,15 @@ typedef struct t1m_group t1m_group;
  * T1M_ERR_KERNEL_TIMEOUT; the context stays usable.  Outputs of such a
  * launch are undefined. */
 #define T1M_GROUP_INJECT_UNMET_DEPENDENCY 4u
+/* complex64 batches as one persistent launch (see above). */
+#define T1M_GROUP_ONE_LAUNCH 8u
+/* One-launch batches: every item's tile forced to 16, 32, 64 or 128 output
+ * columns on the tensor cores (exactly one of these bits; tests and
+ * measurements). */
+#define T1M_GROUP_TILE_16 16u
+#define T1M_GROUP_TILE_32 32u
+#define T1M_GROUP_TILE_64 64u
+#define T1M_GROUP_TILE_128 128u
 
 int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_group_item* items,
                      uint32_t options, t1m_group** group);

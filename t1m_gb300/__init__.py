@@ -127,6 +127,8 @@ class GroupItem(C.Structure):
 GROUP_GRAPH = 1
 GROUP_AUTOTUNE = 2
 GROUP_INJECT_UNMET_DEPENDENCY = 4
+GROUP_ONE_LAUNCH = 8
+GROUP_TILE_16, GROUP_TILE_32, GROUP_TILE_64, GROUP_TILE_128 = 16, 32, 64, 128
 
 _lib_handle: C.CDLL | None = None
 

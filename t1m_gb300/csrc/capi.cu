@@ -1419,6 +1419,26 @@ bool tuned_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
   return true;
 }
 
+// Main-product chunk length of a one-launch item (log2 of stages): narrow
+// outputs (at most 32 columns, the long-K reductions of a sweep's second
+// steps, whose outputs are sums of many terms of either sign) fold every
+// stage, which keeps the truncation bias of the tensor cores' accumulation
+// per chunk at 4 MMAs instead of 16; their converters fold at most 32
+// columns, so the extra folds cost little.  Wider tiles keep four stages.
+int group_fold_shift(int tile_n) { return tile_n <= 32 ? 0 : 2; }
+
+// Tile choice of a one-launch item: a tensor-core width or a SIMT tile.
+constexpr int kWidthSimt = 1;
+bool prepare_group_tc(const GemmArgs& g, const HostPlan& hp, int splits, int width,
+                      TcProblem* tp) {
+  const bool simt = width == kWidthSimt;
+  if (simt && hp.N > kTcSkinnyMaxN) return false;
+  if (!tc_prepare(g, hp, splits, tp, simt ? 16 : width)) return false;
+  tp->skinny = simt ? 1 : 0;
+  tp->fold_shift = group_fold_shift(tp->tile_n);
+  return true;
+}
+
 // Default family before (or without) tuning.
 int heuristic_family(int dtype, const HostPlan& hp) {
   if (dtype == T1M_COMPLEX64 && hp.M >= 32 && hp.N >= 32) return kFamTC;
@@ -1434,7 +1454,9 @@ struct t1m_group {
   double flops = 0;
   void* vectors = nullptr;      // all scatter vectors of all items
   void* tc_dev = nullptr;       // TcProblem array
-  int* done = nullptr;          // tile-completion counters (single TC launch)
+  int* done = nullptr;          // tile-completion counters, then split-K arrival counters
+  int64_t fix_count = 0;        // split-K arrival counters (after the tc_count done counters)
+  bool deps = false;            // the single launch resolves dependencies (cooperative)
   void* simt_dev = nullptr;     // SimtProblem arrays, per (level, family)
   void* reduce_dev = nullptr;   // SplitReduce arrays, per level
   void* work = nullptr;         // split-K partials of all split items
@@ -1461,10 +1483,13 @@ int enqueue_group(t1m_group* g, cudaStream_t s) {
   cudaError_t e = cudaSuccess;
   int kernels = 0;
   if (g->single_tc) {
-    e = cudaMemsetAsync(g->done, 0, sizeof(int) * size_t(std::max(1, g->tc_count)), s);
+    // Counters start at zero every launch (the fix counters also reset
+    // themselves in the kernel; a launch cut short by a timeout may not).
+    e = cudaMemsetAsync(g->done, 0, sizeof(int) * size_t(g->tc_count + g->fix_count), s);
     if (e == cudaSuccess)
       e = tc_launch_persistent(nullptr, static_cast<const TcProblem*>(g->tc_dev), g->tc_count,
-                               g->tc_total, ctx->num_sms, g->done, s, ctx->d_err);
+                               g->tc_total, ctx->num_sms, g->deps ? g->done : nullptr, s,
+                               ctx->d_err, g->fix_count ? g->done + g->tc_count : nullptr);
     kernels = 1;
   } else {
     for (auto& lev : g->levels) {
@@ -1568,6 +1593,26 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
     g->flops += (dtype >= T1M_COMPLEX64 ? 8.0 : 2.0) * double(hp.M) * double(hp.N) * double(hp.K);
   }
 
+  // One persistent launch (T1M_GROUP_ONE_LAUNCH): a complex64 batch runs
+  // every item on the persistent tensor-core kernel, each with its own tile;
+  // dependencies and split-K reductions are resolved inside the kernel.
+  // Measured on the sweep batch of 1024 updates: 159 ms against 128 ms as
+  // family launches per level, because the second steps (N <= 4, A streamed
+  // once) run as SIMT tiles at 47 ms against 22 ms on the skinny kernel
+  // (its two CTAs per SM keep 160 KB of A in flight; the persistent kernel's
+  // four raw stages hold 32 KB), so the family launches stay the default.
+  const bool one_launch = n > 0 && dtype == T1M_COMPLEX64 && ctx->method != T1M_METHOD_PLAIN &&
+                          (options & T1M_GROUP_ONE_LAUNCH);
+  // Tile per item: an output width (16, 32, 64 or 128 columns on the tensor
+  // cores) or kWidthSimt (outputs of at most kTcSkinnyMaxN columns as SIMT
+  // tiles of the same kernel).
+  std::vector<int> width(n, 128);
+  if (one_launch)
+    for (int i = 0; i < n; ++i) {
+      family[i] = kFamTC;
+      width[i] = plans[i].N <= kTcSkinnyMaxN ? kWidthSimt : tc_default_tile_n(plans[i].N);
+    }
+
   // Scatter vectors of every item, one allocation.
   e = cudaMalloc(&g->vectors, std::max<size_t>(vec_elems, 1) * sizeof(int64_t));
   if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group scatter vectors");
@@ -1615,9 +1660,84 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
     if (e != cudaSuccess) return cuda_fail(ctx, e, "group scatter vectors upload");
   }
 
-  // Autotuning: per shape class, time the candidate families once on a
-  // representative item (into a scratch output) and keep the fastest.
-  if (options & T1M_GROUP_AUTOTUNE) {
+  // Autotuning of a one-launch batch: per shape class, time the tile widths
+  // up to the output's width once on a representative item (main kernel
+  // only, with its split count, into a scratch output) and keep the fastest.
+  if (one_launch && (options & T1M_GROUP_AUTOTUNE)) {
+    std::lock_guard<std::mutex> lock(g_tune.mu);
+    g_tune.load(ctx->device);
+    bool changed = false;
+    for (int i = 0; i < n; ++i) {
+      const HostPlan& hp = plans[i];
+      if (hp.M == 0 || hp.N == 0 || hp.K == 0) continue;
+      const std::string key = "w" + shape_class(dtype, hp);
+      auto it = g_tune.choice.find(key);
+      if (it != g_tune.choice.end()) {
+        width[i] = it->second;
+        continue;
+      }
+      int64_t kps = 0;
+      const int nsp = group_splits(dtype, kFamTC, hp, es, &kps);
+      void* scratch = nullptr;
+      if (cudaMalloc(&scratch, size_t(nsp) * size_t(hp.M) * size_t(hp.N) * es) != cudaSuccess)
+        return fail(ctx, T1M_ERR_ALLOC, "autotune scratch");
+      const GemmArgs probe = split_args(args[i], scratch, kps);
+      float best = 1e30f;
+      int best_w = width[i];
+      std::vector<int> cands;
+      if (hp.N <= kTcSkinnyMaxN) cands.push_back(kWidthSimt);
+      for (int w : kTcTileWidths) {
+        if (w > 16 && w / 2 >= hp.N) break;  // wider than the output needs
+        cands.push_back(w);
+      }
+      for (int w : cands) {
+        TcProblem tp;
+        if (!prepare_group_tc(probe, hp, nsp, w, &tp)) continue;
+        tp.dep = -1;
+        float total = 0;
+        bool ok = true;
+        for (int rep = 0; rep < 3 && ok; ++rep) {
+          cudaEventRecord(ctx->ev[4], ctx->stream);
+          const cudaError_t le = tc_launch_persistent(&tp, nullptr, 1, tc_problem_tiles(tp),
+                                                      ctx->num_sms, nullptr, ctx->stream,
+                                                      ctx->d_err);
+          cudaEventRecord(ctx->ev[5], ctx->stream);
+          if (le != cudaSuccess || cudaEventSynchronize(ctx->ev[5]) != cudaSuccess) {
+            cudaGetLastError();
+            ok = false;
+            break;
+          }
+          float ms = 0;
+          cudaEventElapsedTime(&ms, ctx->ev[4], ctx->ev[5]);
+          if (rep > 0) total += ms;  // first run warms up
+        }
+        if (ok && total < best) {
+          best = total;
+          best_w = w;
+        }
+      }
+      cudaFree(scratch);
+      if (int st = check_device_error(ctx)) return st;
+      width[i] = best_w;
+      g_tune.choice[key] = best_w;
+      changed = true;
+    }
+    if (changed) g_tune.save();
+  }
+
+  // A forced tile width (T1M_GROUP_TILE_*).
+  if (const uint32_t fw = options & (T1M_GROUP_TILE_16 | T1M_GROUP_TILE_32 | T1M_GROUP_TILE_64 |
+                                     T1M_GROUP_TILE_128)) {
+    if (fw != T1M_GROUP_TILE_16 && fw != T1M_GROUP_TILE_32 && fw != T1M_GROUP_TILE_64 &&
+        fw != T1M_GROUP_TILE_128)
+      return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "more than one tile width option");
+    std::fill(width.begin(), width.end(), static_cast<int>(fw));
+  }
+
+  // Autotuning of family launches: per shape class, time the candidate
+  // families once on a representative item (into a scratch output) and keep
+  // the fastest.
+  if (!one_launch && (options & T1M_GROUP_AUTOTUNE)) {
     std::lock_guard<std::mutex> lock(g_tune.mu);
     g_tune.load(ctx->device);
     bool changed = false;
@@ -1740,11 +1860,11 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
     if (splits[i] > 1)
       main_args[i] = split_args(args[i], static_cast<char*>(g->work) + work_off[i], kps[i]);
 
-  // Launch lists.  One persistent tensor-core launch for everything if every
-  // item is an unsplit tensor-core item (dependencies resolved in the
-  // kernel), otherwise per level one launch per family, then one grouped
-  // split-K reduction.
-  bool all_tc = n > 0 && !any_split;
+  // Launch lists.  A one-launch batch (and any batch whose items all run on
+  // the tensor cores) is ONE persistent launch: dependencies and split-K
+  // reductions resolved in the kernel.  Otherwise per level one launch per
+  // family, then one grouped split-K reduction.
+  bool all_tc = n > 0;
   for (int i = 0; i < n; ++i) all_tc = all_tc && family[i] == kFamTC;
   int max_level = 0;
   for (int i = 0; i < n; ++i) max_level = std::max(max_level, level[i]);
@@ -1752,6 +1872,69 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
   std::vector<SimtProblem> simts;
   std::vector<SplitReduce> reds;
   std::vector<int> tc_index(n, -1);
+  if (all_tc) {
+    // Tile list order: an item that reads another item's C is placed after
+    // the next independent item that follows its dependency, so its tiles
+    // rarely wait on tiles still in flight (and find part of that C in L2).
+    // Dependent items wait in input order; after an independent item is
+    // placed, every waiting item whose dependency was placed before it
+    // follows.  A dependency always precedes its dependent: it has a smaller
+    // index, so it is placed first or waits ahead of it.
+    std::vector<int> order, waiting;
+    std::vector<int64_t> pos(n, -1);
+    order.reserve(n);
+    auto place = [&](int i) {
+      pos[i] = static_cast<int64_t>(order.size());
+      order.push_back(i);
+    };
+    for (int i = 0; i < n; ++i) {
+      if (items[i].depends_on >= 0) {
+        waiting.push_back(i);
+        continue;
+      }
+      const int64_t here = static_cast<int64_t>(order.size());
+      place(i);
+      std::vector<int> keep;
+      for (int w : waiting) {
+        const int64_t dp = pos[items[w].depends_on];
+        if (dp >= 0 && dp < here) place(w);
+        else keep.push_back(w);
+      }
+      waiting.swap(keep);
+    }
+    for (int w : waiting) place(w);
+    for (int i : order) {
+      const HostPlan& hp = plans[i];
+      TcProblem tp;
+      if (!prepare_group_tc(main_args[i], hp, splits[i], width[i], &tp))
+        return fail(ctx, T1M_ERR_UNSUPPORTED, "group item " + std::to_string(i) +
+                                                  " cannot run on the tensor cores");
+      tp.tile_begin = g->tc_total;
+      tp.dep = -1;
+      tp.dep_tiles = 0;
+      tp.dep_wait_cycles = ctx->wait_limit_us * (ctx->clock_khz / 1000);
+      if (splits[i] > 1) {
+        // In-kernel split-K reduction into the item's own output.
+        tp.fix_begin = g->fix_count;
+        g->fix_count += int64_t(tp.tiles_m) * tp.tiles_n;
+        tp.out = args[i];
+      }
+      if (items[i].depends_on >= 0) {
+        const TcProblem& d = tcs[tc_index[items[i].depends_on]];
+        tp.dep = tc_index[items[i].depends_on];
+        // Only final tiles count: every output tile of the dependency once.
+        tp.dep_tiles = d.tiles_m * d.tiles_n;
+        // Test aid: a count the dependency never reaches.
+        if (options & T1M_GROUP_INJECT_UNMET_DEPENDENCY) ++tp.dep_tiles;
+        g->deps = true;
+      }
+      tc_index[i] = static_cast<int>(tcs.size());
+      g->tc_total += tc_problem_tiles(tp);
+      tcs.push_back(tp);
+    }
+    g->single_tc = true;
+    max_level = -1;  // no level launches
+  }
   g->levels.assign(max_level + 1, {});
   for (int lv = 0; lv <= max_level; ++lv) {
     for (int fam : {kFamTC, kFamSimt, kFamSimtSkinny}) {
@@ -1771,17 +1954,10 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
           if (!tc_prepare(main_args[i], hp, splits[i], &tp))
             return fail(ctx, T1M_ERR_UNSUPPORTED, "group item " + std::to_string(i) +
                                                       " cannot run on the tensor cores");
-          tp.tile_begin = (all_tc ? g->tc_total : L.tiles);
+          tp.tile_begin = L.tiles;
           tp.dep = -1;
           tp.dep_tiles = 0;
           tp.dep_wait_cycles = ctx->wait_limit_us * (ctx->clock_khz / 1000);
-          if (all_tc && items[i].depends_on >= 0) {
-            const TcProblem& d = tcs[tc_index[items[i].depends_on]];
-            tp.dep = tc_index[items[i].depends_on];
-            tp.dep_tiles = static_cast<int32_t>(tc_problem_tiles(d));
-            // Test aid: a count the dependency never reaches.
-            if (options & T1M_GROUP_INJECT_UNMET_DEPENDENCY) ++tp.dep_tiles;
-          }
           tc_index[i] = static_cast<int>(tcs.size());
           const int64_t t = tc_problem_tiles(tp);
           L.tiles += t;
@@ -1817,14 +1993,15 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
     }
     if (R.count > 0) g->levels[lv].push_back(R);
   }
-  g->single_tc = all_tc && max_level > 0;
   g->tc_count = static_cast<int>(tcs.size());
-  if (all_tc && max_level == 0) g->single_tc = false;  // one level: plain persistent launch
   if (!tcs.empty()) {
     e = cudaMalloc(&g->tc_dev, tcs.size() * sizeof(TcProblem));
     if (e == cudaSuccess)
       e = cudaMemcpy(g->tc_dev, tcs.data(), tcs.size() * sizeof(TcProblem), cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMalloc(&g->done, sizeof(int) * tcs.size());
+    if (e == cudaSuccess)
+      e = cudaMalloc(&g->done, sizeof(int) * size_t(int64_t(tcs.size()) + g->fix_count));
+    if (e == cudaSuccess)
+      e = cudaMemset(g->done, 0, sizeof(int) * size_t(int64_t(tcs.size()) + g->fix_count));
     if (e != cudaSuccess) return fail(ctx, T1M_ERR_ALLOC, "group descriptors");
   }
   if (!reds.empty()) {

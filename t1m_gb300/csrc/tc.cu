@@ -79,6 +79,8 @@ constexpr int kStepK = 16;      // complex K per stage = 32 TF32 = one 128 B swi
 constexpr int kRaw = 4;         // raw tile stages
 constexpr int kStages = 2;      // converted operand stages
 constexpr int kFold = 4;        // stages per chunk accumulator (128 real K)
+constexpr int kSkinnyTcN = 8;   // columns of a SIMT tile of the persistent kernel
+static_assert(kSkinnyTcN == kTcSkinnyMaxN, "SIMT tile width");
 constexpr int kThreads = 384;   // warp 0: MMA; warps 1-3: loaders; 4-11: converters
 constexpr int kLoaderBase = 32;
 constexpr int kLoaders = 96;
@@ -97,7 +99,6 @@ constexpr int kBHalfBytes = kTileN * 128;          // B hi (or lo): 128 rows x 1
 constexpr int kOpBytes = 2 * kBHalfBytes;
 constexpr int kBarrierBytes = 256;
 constexpr int kSmemBytes = 1024 + kRaw * kRawBytes + kStages * kOpBytes + kBarrierBytes;
-constexpr uint32_t kIdesc = ptx::idesc_f32acc(2u /*TF32*/, 128, kTileN);
 
 constexpr uint32_t kRegsLaunch = 168;   // 65536 / 384, rounded down to a multiple of 8
 constexpr uint32_t kRegsControl = 96;   // warpgroup 0: MMA issue + loaders
@@ -254,7 +255,8 @@ __device__ __forceinline__ void gather_a_stage(const GemmArgs& g, uint32_t dst, 
 
 template <int kBatch>
 __device__ __forceinline__ void gather_b_stage(const GemmArgs& g, uint32_t dst, int lt,
-                                               int64_t n0, int64_t k0, int64_t ke) {
+                                               int64_t n0, int64_t k0, int64_t ke,
+                                               int tile_n = kTileN) {
   const float2* __restrict__ B = static_cast<const float2*>(g.B);
   const int64_t* __restrict__ csB = g.csB;
   const int64_t uB_n = g.uB_n, N = g.N;
@@ -262,22 +264,22 @@ __device__ __forceinline__ void gather_b_stage(const GemmArgs& g, uint32_t dst, 
   const bool kin = k0 + k < ke;
   const int64_t rk = kin ? offs(g.rsB, g.uB_k, k0 + k) : 0;
   constexpr int kStride = kLoaders / kStepK;                     // 6
-  constexpr int kPer = (kTileN + kStride - 1) / kStride;         // 22
+  const int per = (tile_n + kStride - 1) / kStride;              // 22 for 128 columns
 #pragma unroll 1
-  for (int i0 = 0; i0 < kPer; i0 += kBatch) {
+  for (int i0 = 0; i0 < per; i0 += kBatch) {
     const float2* src[kBatch];
     uint32_t okm = 0;
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const int n = (lt >> 4) + kStride * (i0 + j);
-      const bool in = kin && (i0 + j < kPer) && n < kTileN && (n0 + n < N);
+      const bool in = kin && (i0 + j < per) && n < tile_n && (n0 + n < N);
       src[j] = in ? B + rk + offs(csB, uB_n, n0 + n) : B;
       okm |= in ? (1u << j) : 0u;
     }
 #pragma unroll
     for (int j = 0; j < kBatch; ++j) {
       const int n = (lt >> 4) + kStride * (i0 + j);
-      if (i0 + j < kPer && n < kTileN)
+      if (i0 + j < per && n < tile_n)
         ptx::cp_async_8(dst + swz128(n, k), src[j], ((okm >> j) & 1u) ? 8u : 0u);
     }
   }
@@ -365,7 +367,8 @@ __device__ __forceinline__ void gather_b_stage_real(const GemmArgs& g, uint32_t 
 template <int kCols>
 __device__ __forceinline__ void store_tile(const GemmArgs& g, float2* __restrict__ Cp,
                                            int64_t row, bool row_ok, int64_t n0, int col0,
-                                           int part, const float (&master)[kCols]) {
+                                           int part, const float (&master)[kCols],
+                                           int64_t n_end = INT64_MAX) {
   const uint32_t flags = g.flags;
   const bool accumulate = flags & kFlagAccumulate;
   const bool beta_zero = flags & kFlagBetaZero;
@@ -373,7 +376,7 @@ __device__ __forceinline__ void store_tile(const GemmArgs& g, float2* __restrict
   const bool col16 = flags & kFlagCCol16;
   const float ar = (float)g.alpha[0], ai = (float)g.alpha[1];
   const float br = (float)g.beta[0], bi = (float)g.beta[1];
-  const int64_t N = g.N;
+  const int64_t N = min(g.N, n_end);  // columns of this tile: [n0, N)
   const int64_t* __restrict__ csC = g.csC;
   const int64_t uC_n = g.uC_n;
   const int64_t rowC = row_ok ? offs(g.rsC, g.uC_m, row) : 0;
@@ -492,11 +495,15 @@ __device__ __forceinline__ void store_tile_real(const GemmArgs& g, float* __rest
   }
 }
 
-// Position of one output tile in the tile list.
+// Position of one output tile in the tile list.  tn: the problem's tile
+// width; out_tile: index of the output tile within its split (its fix
+// counter is p->fix_begin + out_tile).
 struct TileRef {
   const TcProblem* p;
   int pi;
-  int64_t m0, n0, kb, ke, ksteps;
+  int tn;
+  int fsh;  // log2 of the stages per main chunk (p->fold_shift)
+  int64_t m0, n0, kb, ke, ksteps, out_tile;
 };
 
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -515,17 +522,19 @@ __device__ __forceinline__ void converters_sync() {
 }
 
 // Tiles of problem p are numbered split-major; within a split, groups of 16
-// M-tiles sweep N so CTAs running together share B in L2.
+// M-tiles sweep N so CTAs running together share B in L2.  Every role of a
+// CTA walks its tiles in increasing order, so the problem is found by a
+// forward scan from the previous tile's (`hint`): usually one load of the
+// next descriptor's tile_begin, where a binary search over a batch of
+// thousands of problems took a dozen dependent loads per tile and role.
 __device__ __forceinline__ TileRef locate(const TcProblem* single, const TcProblem* group,
-                                          int nprob, int64_t t) {
+                                          int nprob, int64_t t, int& hint) {
   const TcProblem* p = single;
   int lo = 0;
   if (group) {
-    int hi = nprob - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (group[mid].tile_begin <= t) lo = mid; else hi = mid - 1;
-    }
+    lo = hint;
+    while (lo + 1 < nprob && group[lo + 1].tile_begin <= t) ++lo;
+    hint = lo;
     p = group + lo;
   }
   const int64_t lt = t - p->tile_begin;
@@ -541,18 +550,68 @@ __device__ __forceinline__ TileRef locate(const TcProblem* single, const TcProbl
   TileRef ref;
   ref.p = p;
   ref.pi = lo;
+  ref.tn = p->tile_n;
+  ref.fsh = p->fold_shift;
+  ref.out_tile = r;
   ref.m0 = tm * kTileMc;
-  ref.n0 = tn * kTileN;
+  ref.n0 = tn * p->tile_n;
   ref.kb = split * p->g.k_per_split;
   ref.ke = min(p->g.K, ref.kb + p->g.k_per_split);
   ref.ksteps = (ref.ke - ref.kb + kStepK - 1) / kStepK;
   return ref;
 }
 
+// In-kernel split-K reduction of one output tile (the converter warps of the
+// split that arrived last, pt = 0..255): C(m, n) <- alpha * sum_s W_s(m, n)
+// + beta * C(m, n) (or C + alpha * sum), the sum over the splits in order
+// and the epilogue in FP64, as the separate reduction kernel does.  The
+// partials are the raw products written through p.g (dense, uniform
+// strides, c_split_stride apart); other CTAs wrote them, so they are read
+// from L2 (ld.global.cg).  Thread pt takes row m0 + pt % 64 and columns
+// n0 + pt / 64, + 4, ... of the tile.
+__device__ __noinline__ void fix_reduce_tile(const TcProblem& p, const TileRef& tr, int pt) {
+  const GemmArgs& w = p.g;
+  const GemmArgs& o = p.out;
+  const int64_t m = tr.m0 + (pt & 63);
+  if (m >= w.M) return;
+  const int64_t n_end = min(w.N, tr.n0 + tr.tn);
+  const float2* __restrict__ W = static_cast<const float2*>(w.C);
+  const int64_t wm = m * w.uC_m;
+  const int64_t om = offs(o.rsC, o.uC_m, m);
+  const int splits = p.splits;
+  const double ar = o.alpha[0], ai = o.alpha[1], br = o.beta[0], bi = o.beta[1];
+  for (int64_t n = tr.n0 + (pt >> 6); n < n_end; n += 4) {
+    const float2* src = W + wm + n * w.uC_n;
+    double sr = 0.0, si = 0.0;
+#pragma unroll 4
+    for (int sp = 0; sp < splits; ++sp) {
+      const float2 v = __ldcg(src + static_cast<int64_t>(sp) * w.c_split_stride);
+      sr += static_cast<double>(v.x);
+      si += static_cast<double>(v.y);
+    }
+    float2* dst = static_cast<float2*>(o.C) + om + offs(o.csC, o.uC_n, n);
+    double rr = ar * sr - ai * si, ri = ar * si + ai * sr;
+    if (o.flags & kFlagAccumulate) {
+      const float2 c = *dst;
+      rr += c.x;
+      ri += c.y;
+    } else if (!(o.flags & kFlagBetaZero)) {
+      const float2 c = *dst;
+      rr += br * c.x - bi * c.y;
+      ri += br * c.y + bi * c.x;
+    }
+    *dst = make_float2(static_cast<float>(rr), static_cast<float>(ri));
+  }
+}
+
 __global__ void __launch_bounds__(kThreads, 1)
 tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* group, int nprob,
-                    int64_t total_tiles, int* done, int* err_flag) {
+                    int64_t total_tiles, int* done, int* err_flag, int* fix) {
   extern __shared__ __align__(16) uint8_t smem_raw[];
+  __shared__ int s_fix_last;  // in-kernel split-K: this CTA's split arrived last
+  // SIMT tiles: B columns of a stage, k-major, double-buffered (rows padded
+  // so the four k a warp reads at once fall in different banks).
+  __shared__ float2 s_skb[2][kStepK][kSkinnyTcN + 1];
   const uint32_t base = (ptx::smem_u32(smem_raw) + 1023u) & ~1023u;
   uint8_t* const base_ptr = smem_raw + (base - ptx::smem_u32(smem_raw));
   const uint32_t raw0 = base;                          // kRaw x (A 8 KB | B 16 KB)
@@ -619,9 +678,14 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
     // ---------------------------------------------------------- MMA issue ---
     if (lane == 0) {
       bool ok = true;
-      int64_t op_cnt = 0, chunk_cnt = 0, tile_cnt = 0;
-      for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++tile_cnt) {
-        const TileRef tr = locate(&single, group, nprob, t);
+      int64_t op_cnt = 0, chunk_cnt = 0, tile_cnt = 0;  // tile_cnt: tensor-core tiles
+      int hint = 0;
+      for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
+        const TileRef tr = locate(&single, group, nprob, t, hint);
+        // SIMT tiles (narrow outputs) are computed by the converter warps
+        // alone: no MMA, no TMEM, none of this thread's barriers.
+        if (tr.p->skinny) continue;
+        const uint32_t idesc = ptx::idesc_f32acc(2u /*TF32*/, 128, static_cast<uint32_t>(tr.tn));
         // The previous tile's epilogue must have read the accumulators.
         if (tile_cnt > 0 && !ptx::mbar_wait(acc_empty, static_cast<uint32_t>((tile_cnt - 1) & 1))) {
           record_error(err_flag, kErrAccEmptyWait);
@@ -631,7 +695,8 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         for (int64_t s = 0; s < tr.ksteps; ++s, ++op_cnt) {
           const int st = static_cast<int>(op_cnt % kStages);
           const uint32_t ph = static_cast<uint32_t>((op_cnt / kStages) & 1);
-          const bool chunk_start = (s % kFold) == 0;
+          const int64_t fmask = (int64_t(1) << tr.fsh) - 1;
+          const bool chunk_start = (s & fmask) == 0;
           if (chunk_start && s > 0) ++chunk_cnt;
           const int buf = static_cast<int>(chunk_cnt & 1);
           if (chunk_start && chunk_cnt >= 2 &&
@@ -656,16 +721,17 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           for (int kk = 0; kk < 4; ++kk) {
             const uint64_t dh = ptx::smem_desc_sw128(b_hi + 32u * kk);
             const uint64_t dl = ptx::smem_desc_sw128(b_lo + 32u * kk);
-            ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, kIdesc, (chunk_start && kk == 0) ? 0u : 1u);
-            ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, kIdesc, (s == 0 && kk == 0) ? 0u : 1u);
-            ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, kIdesc, 1u);
+            ptx::mma_tf32_ts(d_main, a_hi + 8u * kk, dh, idesc, (chunk_start && kk == 0) ? 0u : 1u);
+            ptx::mma_tf32_ts(d_corr, a_hi + 8u * kk, dl, idesc, (s == 0 && kk == 0) ? 0u : 1u);
+            ptx::mma_tf32_ts(d_corr, a_lo + 8u * kk, dh, idesc, 1u);
           }
           ptx::mma_commit(empty_bar(st));
-          if ((s % kFold) == kFold - 1 || s == tr.ksteps - 1) ptx::mma_commit(chunk_full(buf));
+          if ((s & fmask) == fmask || s == tr.ksteps - 1) ptx::mma_commit(chunk_full(buf));
         }
         if (!ok) break;
         ++chunk_cnt;  // the next tile starts a fresh chunk
         ptx::mma_commit(acc_full);
+        ++tile_cnt;
       }
       // Make sure no MMA is still writing TMEM before it is freed.
       if (tile_cnt > 0 && !ptx::mbar_wait(acc_full, static_cast<uint32_t>((tile_cnt - 1) & 1)))
@@ -680,9 +746,10 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
     // ------------------------------------------------------------ loaders ---
     const int lt = tid - kLoaderBase;  // 0..95
     int64_t raw_cnt = 0;
+    int hint = 0;
     bool dep_failed = false;  // a dependency wait of this thread ran out
     for (int64_t t = blockIdx.x; t < total_tiles; t += gridDim.x) {
-      const TileRef tr = locate(&single, group, nprob, t);
+      const TileRef tr = locate(&single, group, nprob, t, hint);
       const TcProblem* p = tr.p;
       const GemmArgs& g = p->g;
       const int amode = p->amode, bmode = p->bmode;
@@ -702,9 +769,11 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
           const int64_t n = tr.n0 + 16 * j;
-          colb[j] = n < g.N ? offs(g.csB, g.uB_n, n) : 0;
+          colb[j] = (16 * j < tr.tn && n < g.N) ? offs(g.csB, g.uB_n, n) : 0;
         }
       }
+      // The B stage holds tn rows (columns of the output tile).
+      const uint32_t b_bytes = static_cast<uint32_t>(tr.tn) * (kRawBBytes / kTileN);
       // Tiles fetched entirely by TMA need only the TMA thread; the other
       // loader threads skip them (the TMA thread arrives on their behalf).
       const bool gathering = amode == kAGather || bmode == kBGather;
@@ -757,7 +826,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         }
         if (lt == 0) {
           const uint32_t bytes = (amode != kAGather ? kRawABytes : 0) +
-                                 (bmode != kBGather ? kRawBBytes : 0);
+                                 (bmode != kBGather ? b_bytes : 0);
           ptx::mbar_arrive_expect_tx(raw_full(r), bytes);
           if (amode == kAMK)
             ptx::tma_load_2d(raw_a(r), &p->map_a, static_cast<int>(2 * tr.m0), static_cast<int>(k0), raw_full(r));
@@ -790,8 +859,9 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
             const int64_t rk = offs(g.rsB, g.uB_k, k0);
 #pragma unroll
             for (int j = 0; j < 8; ++j)
-              ptx::tma_load_2d(raw_b(r) + 2048u * j, &p->map_b, static_cast<int>(2 * (colb[j] + rk)),
-                               0, raw_full(r));
+              if (16 * j < tr.tn)
+                ptx::tma_load_2d(raw_b(r) + 2048u * j, &p->map_b,
+                                 static_cast<int>(2 * (colb[j] + rk)), 0, raw_full(r));
           }
           if (bmode == kBKN)
             ptx::tma_load_2d(raw_b(r), &p->map_b, static_cast<int>(2 * tr.n0), static_cast<int>(k0), raw_full(r));
@@ -801,7 +871,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
           }
         }
         if (amode == kAGather) gather_a_stage<2>(g, raw_a(r), lt, tr.m0, k0, tr.ke);
-        if (bmode == kBGather) gather_b_stage<2>(g, raw_b(r), lt, tr.n0, k0, tr.ke);
+        if (bmode == kBGather) gather_b_stage<2>(g, raw_b(r), lt, tr.n0, k0, tr.ke, tr.tn);
         ptx::cp_async_arrive_noinc(raw_full(r));
       }
       if (stop) break;
@@ -817,9 +887,13 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
     const uint32_t lane_base = static_cast<uint32_t>(32 * q) << 16;
 
     float master[64];
+    // Columns of the current tile (its width): accumulator columns past it
+    // hold nothing of this tile and are not read.
+    int cur_tn = kTileN;
     auto fold_from = [&](uint32_t col) {
 #pragma unroll
       for (int cc = 0; cc < 2; ++cc) {
+        if (64 * wg + 32 * cc >= cur_tn) break;  // warp-uniform
         uint32_t r[32];
         ptx::tmem_ld32_sync(tmem + lane_base + col + 64u * wg + 32u * cc, r);
 #pragma unroll
@@ -859,18 +933,34 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       // B: piece j of this thread is piece 0 plus kBStep j bytes in the raw
       // tile (and for [n][k] 4096 j in the swizzled operand tile).  In the
       // [k][n] forms piece j is k = (pt >> 6) + 4 j, columns n, n + 1.
+      // The tile's B has tr.tn rows: a [k][n] stage (TMA box [16 k][tn n])
+      // has rows of tn complex, and pieces past tn are neither read nor
+      // converted (the MMA reads tn rows).
       constexpr bool kBRowsK = BL == 1 || BL == 3;
-      constexpr uint32_t kBStep = BL == 3 ? 512u : 4096u;
-      const int bn = 2 * (pt & 63), bk = pt >> 6;
+      const int tn = tr.tn;
+      const uint32_t bpitch = static_cast<uint32_t>(tn) * 8u;
+      const uint32_t kBStep = BL == 3 ? 512u : BL == 1 ? 4u * bpitch : 4096u;
+      // [k][n] raw tiles: warp w takes columns 16 w .. 16 w + 15 (two per
+      // lane) and k = lane % 4 (+ 4 j): per store instruction the warp's
+      // 32 lanes then write 8-byte pieces into all eight 16-byte chunks of
+      // the 128-byte swizzled rows (two lanes per slot, the minimum), where
+      // k fixed per warp put all of them in four chunks (8-way conflicts).
+      const int bn = kBRowsK ? 16 * (pt >> 5) + 2 * ((pt & 31) >> 2) : 0;
+      const int bk = kBRowsK ? (pt & 3) : 0;
       const uint32_t bsrc0 =
-          BL == 1 ? static_cast<uint32_t>(bk * 1024 + bn * 8)
+          BL == 1 ? static_cast<uint32_t>(bk * bpitch + bn * 8)
           : BL == 3 ? static_cast<uint32_t>((bn >> 4) * 2048 + bk * 128 + (bn & 15) * 8)
                     : swz128(pt >> 3, 2 * (pt & 7));
+      // Pieces j of this thread inside the tile's tn rows.
+      uint32_t bmask = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (kBRowsK ? bn < tn : (pt >> 3) + 32 * j < tn) bmask |= 1u << j;
       uint32_t boff_kn[4][2];
       if constexpr (kBRowsK) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-          const int k = (pt >> 6) + 4 * j, n = 2 * (pt & 63);
+          const int k = bk + 4 * j, n = bn;
           boff_kn[j][0] = swz128(n, k);
           boff_kn[j][1] = swz128(n + 1, k);
         }
@@ -898,7 +988,8 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         float4 bv[4];
         const uint32_t b0 = rb + bsrc0;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) bv[j] = lds128(b0 + kBStep * j);
+        for (int j = 0; j < 4; ++j)
+          bv[j] = (bmask >> j) & 1u ? lds128(b0 + kBStep * j) : make_float4(0.f, 0.f, 0.f, 0.f);
         // The raw stage is released after the conversion (below), once the
         // values read from it are consumed and behind the cross-proxy fence:
         // TMA (async proxy) refills it, and generic-proxy reads that are not
@@ -936,6 +1027,7 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         const uint32_t ob = op0 + st * kOpBytes;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
+          if (!((bmask >> j) & 1u)) continue;
           float4 v = bv[j];
           if (conjB) {
             v.y = -v.y;
@@ -968,8 +1060,8 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         }
 
         // Fold the previous chunk once the first stage of the next is queued.
-        if ((s % kFold) == 0 && s >= kFold) {
-          const int64_t c = chunk_base + s / kFold - 1;
+        if ((s & ((1 << tr.fsh) - 1)) == 0 && s >= (1 << tr.fsh)) {
+          const int64_t c = chunk_base + (s >> tr.fsh) - 1;
           const int buf = static_cast<int>(c & 1);
           if (!ptx::mbar_wait(chunk_full(buf), static_cast<uint32_t>((c >> 1) & 1))) {
             record_error(err_flag, kErrChunkWait);
@@ -985,14 +1077,140 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       return true;
     };
 
-    for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x, ++tile_cnt) {
-      const TileRef tr = locate(&single, group, nprob, t);
+    // SIMT tiles (TcProblem::skinny: outputs of at most kSkinnyTcN columns):
+    // the converter warps compute the tile's products with FP32 FMAs straight
+    // from the raw stages, which the loaders fill exactly as for tensor-core
+    // tiles; the MMA thread skips the tile.  Thread pt takes row pt / 4 of
+    // the tile and k = kq, kq + 4, kq + 8, kq + 12 of every stage (kq =
+    // pt % 4); per stage the B columns are first copied into s_skb (k-major,
+    // conjugated), and each stage's products are summed on their own before
+    // they are added to the running sums (shorter FP32 sums, smaller error).
+    // The four threads of a row then add their sums (shuffles) and the first
+    // writes the row.  Returns false when a wait ran out.
+    uint32_t sk_cnt = 0;  // SIMT stages processed (s_skb buffer parity)
+    int hint = 0;
+    auto run_skinny = [&](const TileRef& tr, int alay, int blay, bool conjA, bool conjB,
+                          float2* __restrict__ Cp) -> bool {
+      const GemmArgs& g = tr.p->g;
+      const int r = pt >> 2, kq = pt & 3;
+      const int ncols = static_cast<int>(min(g.N - tr.n0, static_cast<int64_t>(kSkinnyTcN)));
+      uint32_t aoff[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int k = kq + 4 * i;
+        aoff[i] = alay == 2 ? swz128(r, k)
+                  : alay == 1 ? static_cast<uint32_t>((r >> 4) * 2048 + k * 128 + (r & 15) * 8)
+                              : static_cast<uint32_t>(k * 512 + r * 8);
+      }
+      // B element copied by this thread (pt < 16 x kSkinnyTcN): k = pt / N', n = pt % N'.
+      const int bk = pt / kSkinnyTcN, bn = pt % kSkinnyTcN;
+      const bool bcopy = pt < kStepK * kSkinnyTcN;
+      const uint32_t boff =
+          blay == 1 ? static_cast<uint32_t>(bk * tr.tn * 8 + bn * 8)
+          : blay == 3 ? static_cast<uint32_t>((bn >> 4) * 2048 + bk * 128 + (bn & 15) * 8)
+                      : swz128(bn, bk);
+      float acc[2 * kSkinnyTcN];
+#pragma unroll
+      for (int j = 0; j < 2 * kSkinnyTcN; ++j) acc[j] = 0.f;
+      const int ksteps = static_cast<int>(tr.ksteps);
+      for (int s = 0; s < ksteps; ++s) {
+        if (!ptx::mbar_wait(raw_full(rr), rph)) {
+          record_error(err_flag, kErrRawWait);
+          return false;
+        }
+        const uint32_t ra = raw_a(rr), rb = raw_b(rr);
+        const int r_cur = static_cast<int>(rr);
+        if (++rr == kRaw) {
+          rr = 0;
+          rph ^= 1u;
+        }
+        // Buffers alternate over all SIMT stages of this CTA (also across
+        // tiles): a buffer is rewritten only after the barrier that follows
+        // its last reads.
+        float2 (*bs)[kSkinnyTcN + 1] = s_skb[sk_cnt++ & 1];
+        if (bcopy) {
+          float2 b = bn < ncols ? lds64(rb + boff) : make_float2(0.f, 0.f);
+          if (conjB) b.y = -b.y;
+          bs[bk][bn] = b;
+        }
+        float2 a[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          a[i] = lds64(ra + aoff[i]);
+          if (conjA) a[i].y = -a[i].y;
+        }
+        converters_sync();  // this stage's B copy is complete
+        float sacc[2 * kSkinnyTcN];
+#pragma unroll
+        for (int j = 0; j < 2 * kSkinnyTcN; ++j) sacc[j] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+#pragma unroll
+          for (int n = 0; n < kSkinnyTcN; ++n) {
+            if (n >= ncols) break;
+            const float2 b = bs[kq + 4 * i][n];
+            sacc[2 * n] = fmaf(a[i].x, b.x, fmaf(-a[i].y, b.y, sacc[2 * n]));
+            sacc[2 * n + 1] = fmaf(a[i].x, b.y, fmaf(a[i].y, b.x, sacc[2 * n + 1]));
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 2 * kSkinnyTcN; ++j) acc[j] += sacc[j];
+        // The stage's values are consumed: release it to the next TMA fill
+        // behind the cross-proxy fence.
+        ptx::fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) ptx::mbar_arrive(raw_empty(r_cur));
+      }
+#pragma unroll
+      for (int j = 0; j < 2 * kSkinnyTcN; ++j) {
+        acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], 1);
+        acc[j] += __shfl_xor_sync(0xffffffffu, acc[j], 2);
+      }
+      const int64_t m = tr.m0 + r;
+      if (kq == 0 && m < g.M) {
+        const bool accumulate = g.flags & kFlagAccumulate;
+        const bool beta_zero = g.flags & kFlagBetaZero;
+        const float ar = (float)g.alpha[0], ai = (float)g.alpha[1];
+        const float br = (float)g.beta[0], bi = (float)g.beta[1];
+        float2* __restrict__ Cr = Cp + offs(g.rsC, g.uC_m, m);
+#pragma unroll
+        for (int n = 0; n < kSkinnyTcN; ++n) {
+          if (n >= ncols) break;
+          const float re = acc[2 * n], im = acc[2 * n + 1];
+          const float tr_ = ar * re - ai * im, ti = ar * im + ai * re;
+          float2* c = Cr + offs(g.csC, g.uC_n, tr.n0 + n);
+          if (accumulate) {
+            const float2 o = *c;
+            *c = make_float2(o.x + tr_, o.y + ti);
+          } else if (beta_zero) {
+            *c = make_float2(tr_, ti);
+          } else {
+            const float2 o = *c;
+            *c = make_float2(tr_ + (br * o.x - bi * o.y), ti + (br * o.y + bi * o.x));
+          }
+        }
+      }
+      return true;
+    };
+
+    for (int64_t t = blockIdx.x; t < total_tiles && ok; t += gridDim.x) {
+      const TileRef tr = locate(&single, group, nprob, t, hint);
       const TcProblem* p = tr.p;
       const GemmArgs& g = p->g;
       const int amode = p->amode, bmode = p->bmode;
       const bool conjA = g.flags & kFlagConjA;
       const bool conjB = g.flags & kFlagConjB;
       const bool row_ok = (tr.m0 + ci) < g.M;
+      const int alay = (amode == kAKM || amode == kAKM16) ? 2
+                       : (amode == kAMK16 || amode == kAMK16K) ? 1 : 0;
+      const int blay = bmode == kBKN ? 1 : (bmode == kBKN16 ? 3 : 0);
+      const int64_t split = tr.kb / g.k_per_split;
+      float2* __restrict__ Cp = static_cast<float2*>(g.C) + split * g.c_split_stride;
+      if (p->skinny) {
+        ok = run_skinny(tr, alay, blay, conjA, conjB, Cp);
+        if (!ok) break;
+      } else {
+      cur_tn = tr.tn;
 #pragma unroll
       for (int j = 0; j < 64; ++j) master[j] = 0.f;
       const int64_t chunk_base = chunk_cnt;
@@ -1000,9 +1218,6 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       using I1 = std::integral_constant<int, 1>;
       using I2 = std::integral_constant<int, 2>;
       using I3 = std::integral_constant<int, 3>;
-      const int alay = (amode == kAKM || amode == kAKM16) ? 2
-                       : (amode == kAMK16 || amode == kAMK16K) ? 1 : 0;
-      const int blay = bmode == kBKN ? 1 : (bmode == kBKN16 ? 3 : 0);
       switch (alay * 4 + blay) {
         case 0: ok = run_stages(I0{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
         case 1: ok = run_stages(I0{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
@@ -1025,10 +1240,15 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
       ptx::tc_fence_after();
       // The last chunk of the tile was not folded in the loop; then the
       // corrections.  After these reads the accumulators are free again.
-      const int64_t c_last = chunk_base + (tr.ksteps - 1) / kFold;
+      const int64_t c_last = chunk_base + (tr.ksteps > 0 ? (tr.ksteps - 1) >> tr.fsh : 0);
       const int buf_last = static_cast<int>(c_last & 1);
-      fold_from(buf_last ? kChunkCol1 : kChunkCol0);
-      fold_from(kCorrCol);
+      // An empty K range (K = 0) leaves the accumulators unwritten: nothing
+      // is folded (C = beta C), but the arrivals below keep the barrier
+      // phases of both sides in step (the MMA thread counts a chunk too).
+      if (tr.ksteps > 0) {
+        fold_from(buf_last ? kChunkCol1 : kChunkCol0);
+        fold_from(kCorrCol);
+      }
       ptx::tc_fence_before();
       __syncwarp();
       if (lane == 0) {
@@ -1036,11 +1256,32 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         ptx::mbar_arrive(acc_empty);
       }
       chunk_cnt = c_last + 1;
+      ++tile_cnt;
 
-      const int64_t split = tr.kb / g.k_per_split;
-      float2* __restrict__ Cp = static_cast<float2*>(g.C) + split * g.c_split_stride;
-      store_tile<64>(g, Cp, tr.m0 + ci, row_ok, tr.n0, wg * 64, part, master);
-      if (done) {
+      if (64 * wg < tr.tn)
+        store_tile<64>(g, Cp, tr.m0 + ci, row_ok, tr.n0, wg * 64, part, master,
+                       tr.n0 + tr.tn);
+      }
+      bool final_tile = true;
+      if (fix && p->fix_begin >= 0) {
+        // In-kernel split-K reduction.  Every converter's partial stores
+        // are made visible device-wide before the one arrival of this split;
+        // the split that arrives last (all others' partials written) sums
+        // the output tile over all splits.
+        __threadfence();
+        converters_sync();
+        if (pt == 0) {
+          int* ctr = fix + p->fix_begin + tr.out_tile;
+          const int last = atomicAdd(ctr, 1) == p->splits - 1;
+          if (last) *ctr = 0;  // every split has arrived: ready for the next launch
+          s_fix_last = last;
+          __threadfence();
+        }
+        converters_sync();
+        final_tile = s_fix_last != 0;
+        if (final_tile) fix_reduce_tile(*p, tr, pt);
+      }
+      if (done && final_tile) {
         // Publish the tile: every converter's stores, then one release-add.
         converters_sync();
         if (pt == 0) {
@@ -1581,8 +1822,13 @@ tc1m_contract(const GemmArgs args, const __grid_constant__ TmaMaps maps, int* er
       const int id = pt + kConverters1 * j;
       if (BMode == kTmaKN) {
         // k: complex k, or (real) the k pair 2k, 2k + 1 (rows of kNCta
-        // complex or 128 real values).
-        const int k = id / (kNCta / 2), n = 2 * (id % (kNCta / 2));
+        // complex or 128 real values).  Warp task w = id / 32 takes k =
+        // 4 (w % 4) + lane % 4 and columns 16 (w / 4) + 2 (lane / 4), + 1:
+        // the warp's 8-byte stores then fill all eight 16-byte chunks of the
+        // swizzled rows (two lanes per slot) instead of four (k fixed per
+        // warp: 8-way bank conflicts).
+        const int w = id >> 5, l = id & 31;
+        const int k = 4 * (w & 3) + (l & 3), n = 16 * (w >> 2) + 2 * (l >> 2);
         bsrc[j] = kReal ? static_cast<uint32_t>(2 * k * 512 + n * 4)
                         : static_cast<uint32_t>(k * kNCta * 8 + n * 8);
         boff[j][0] = swz128(n, k);
@@ -2665,12 +2911,37 @@ bool stride16(const HostPlan& plan, int which, const std::vector<int64_t>& rows,
   return r;
 }
 
-bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p) {
+int tc_default_tile_n(int64_t N) {
+  // Time per stage of 16 complex k and tile of the persistent kernel,
+  // measured over the sweep batch's first steps with every width forced
+  // (16, 32, 64, 128 columns: 5.4, 2.9, 1.6 and 1 times the 128-column
+  // time for 8, 4, 2 and 1 tiles): the A side (loads, 1M split, TMEM
+  // stores) dominates and does not shrink with the width.  Modelled as
+  // 1000 + 3.5 x width clocks.
+  int best = kTileN;
+  double best_cost = 1e300;
+  for (int w : kTcTileWidths) {
+    const double cost = double((N + w - 1) / w) * (1000.0 + 3.5 * w);
+    if (cost < best_cost) {
+      best_cost = cost;
+      best = w;
+    }
+  }
+  return best;
+}
+
+bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p, int tile_n) {
   std::memset(static_cast<void*>(p), 0, sizeof(*p));
+  if (tile_n == 0) tile_n = tc_default_tile_n(g.N);
+  if (tile_n != 16 && tile_n != 32 && tile_n != 64 && tile_n != 128) return false;
   p->g = g;
   p->g.flags = (g.flags & ~(kFlagCPairs | kFlagCCol16)) | c_store_flags(g, plan);
+  p->tile_n = tile_n;
+  p->fold_shift = 2;  // kFold = 4 stages per main chunk
+  p->skinny = 0;
+  p->fix_begin = -1;
   p->tiles_m = static_cast<int32_t>((g.M + kTileMc - 1) / kTileMc);
-  p->tiles_n = static_cast<int32_t>((g.N + kTileN - 1) / kTileN);
+  p->tiles_n = static_cast<int32_t>((g.N + tile_n - 1) / tile_n);
   p->splits = splits;
   if (splits < 1 || (splits > 1 && g.k_per_split % kStepK != 0)) return false;
   if (g.M >= (int64_t(1) << 31) / kTileMc || g.N >= (int64_t(1) << 31) / kTileN) return false;
@@ -2703,14 +2974,16 @@ bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* 
   }
   // B: TMA over a uniform 2-D view or per unit-stride 16-element K block, or gather.
   p->bmode = kBGather;
+  // B boxes are tile_n rows (columns of the output tile) high.
+  const uint32_t tn = static_cast<uint32_t>(tile_n);
   if (plan.uB_k == 1 && plan.uB_n >= 0 &&
-      make_map(&p->map_b, g.B, g.K, g.N, plan.uB_n, 2 * kStepK, kTileN, true))
+      make_map(&p->map_b, g.B, g.K, g.N, plan.uB_n, 2 * kStepK, tn, true))
     p->bmode = kBNK;
   else if (plan.uB_n == 1 && plan.uB_k >= 0 &&
-           make_map(&p->map_b, g.B, g.N, g.K, plan.uB_k, 2 * kTileN, kStepK, false))
+           make_map(&p->map_b, g.B, g.N, g.K, plan.uB_k, 2 * tn, kStepK, false))
     p->bmode = kBKN;
   else if (plan.uB_n >= 0 && g.K % kStepK == 0 && unit16(plan, kChkUnitRsB, plan.rsB, g.K) &&
-           make_map(&p->map_b, g.B, plan.spanB, g.N, plan.uB_n, 2 * kStepK, kTileN, true)) {
+           make_map(&p->map_b, g.B, plan.spanB, g.N, plan.uB_n, 2 * kStepK, tn, true)) {
     p->bmode = kBNK;
     p->block_maps |= 2;
   } else if (int64_t sn = 0; g.K % kStepK == 0 && unit16(plan, kChkUnitRsB, plan.rsB, g.K) &&
@@ -2733,7 +3006,7 @@ int64_t tc_problem_tiles(const TcProblem& p) {
 
 cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_group, int nprob,
                                  int64_t total_tiles, int num_sms, int* done,
-                                 cudaStream_t stream, int* err_flag) {
+                                 cudaStream_t stream, int* err_flag, int* fix) {
   {
     std::lock_guard<std::mutex> lock(g_attr_mutex);
     if (!g_attr_set) {
@@ -2753,13 +3026,13 @@ cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_g
   if (done) {
     // Tiles wait on tiles of other CTAs: all CTAs must be resident.
     void* params[] = {const_cast<TcProblem*>(single), &dev_group, &nprob, &total_tiles, &done,
-                      &err_flag};
+                      &err_flag, &fix};
     return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(tc3xtf32_persistent),
                                        dim3(static_cast<unsigned>(grid)), dim3(kThreads), params,
                                        kSmemBytes, stream);
   }
   tc3xtf32_persistent<<<static_cast<unsigned>(grid), kThreads, kSmemBytes, stream>>>(
-      *single, dev_group, nprob, total_tiles, done, err_flag);
+      *single, dev_group, nprob, total_tiles, done, err_flag, fix);
   return cudaGetLastError();
 }
 
@@ -3119,6 +3392,15 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                packed_args.B != args.B);
     }
   } else {
+    // The persistent kernel takes narrower output tiles where the output
+    // has few columns (abcd,dbea->ec: N = 64 in one 64-column tile instead
+    // of half a 128-column tile).
+    if (const int w = tc_default_tile_n(p.g.N); w != p.tile_n) {
+      TcProblem q;
+      if (tc_prepare(packed_args, *packed_plan, splits, &q, w)) p = q;
+    }
+    p.tile_begin = 0;
+    p.dep = -1;
     mark(0);
     e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
     mark(1);

@@ -50,20 +50,63 @@ struct TcProblem {
   // Bound, in SM clock cycles, on the wait for the dependency's tiles (0:
   // the kernels' default of about two seconds).
   int64_t dep_wait_cycles;
+  // Output tile width in complex (or real) columns: the MMA N and the height
+  // of the B stage, one of 16, 32, 64, 128 (kTcTileWidths).  Narrow outputs
+  // (the second step of a sweep update, N <= 4) take a 16-column tile
+  // instead of computing a 128-column tile of which most is empty.
+  int32_t tile_n;
+  // Stages per main-product chunk accumulator, as a power of two (default
+  // 2: four stages, 16 accumulating MMAs).  The tensor cores' FP32
+  // accumulation truncates, with a bias of about 2e-8 of the accumulator per
+  // accumulating MMA, so shorter chunks (folded into FP32 registers with
+  // round-to-nearest adds) keep outputs that are sums of many terms of
+  // either sign accurate.
+  int32_t fold_shift;
+  // In-kernel split-K reduction (grouped launches): when fix_begin >= 0 the
+  // splits write raw partial products through g (a dense workspace, as for
+  // the separate reduction) and count their arrivals on fix counters
+  // fix_begin + output tile; the split that arrives last sums all partials
+  // of its output tile in FP64, in split order, and applies the epilogue of
+  // `out` (the item's C, alpha, beta and flags).  Only those final tiles
+  // count towards the problem's tile-completion counter.
+  int64_t fix_begin;
+  GemmArgs out;
+  // SIMT tile (tile_n 16, N <= 8): the converter warps compute the products
+  // with FP32 FMAs from the raw stages and the MMA thread skips the tile.  A
+  // narrow output streams A once; on the tensor cores its 1M split of A
+  // would bound it (measured on the sweep batch's second steps: 57 ms as
+  // 16-column tensor-core tiles, against 22 ms on the skinny kernel).
+  int32_t skinny;
+  int32_t pad2_;
 };
+
+// Widest output a SIMT tile of the persistent kernel takes.
+constexpr int kTcSkinnyMaxN = 8;
+
+// Output tile widths of the persistent kernel.
+constexpr int kTcTileWidths[4] = {16, 32, 64, 128};
+// Tile width for an output of N columns when none is given: the cheapest
+// under a per-stage cost model of the persistent kernel (A side fixed, B
+// side and MMA proportional to the width), so narrow outputs get narrow
+// tiles and wide outputs 128 columns.
+int tc_default_tile_n(int64_t N);
 
 // Fill a descriptor (fetch modes, tensor maps, tile counts).  False if the
 // problem cannot run on this kernel.
-bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p);
+// `tile_n`: output tile width (one of kTcTileWidths), 0 = tc_default_tile_n.
+bool tc_prepare(const GemmArgs& g, const HostPlan& plan, int splits, TcProblem* p,
+                int tile_n = 128);
 int64_t tc_problem_tiles(const TcProblem& p);
 // One persistent launch over `total_tiles` tiles of `single` (dev_group null)
 // or of the device array dev_group[0..nprob) (sorted by tile_begin, every
 // dependency's tiles before its dependents').  `done` (grouped launches with
 // dependencies) holds one zeroed tile-completion counter per problem; such
 // launches are cooperative so all CTAs are resident.
+// `fix` holds the zeroed split-K arrival counters of problems with
+// fix_begin >= 0 (null when there are none).
 cudaError_t tc_launch_persistent(const TcProblem* single, const TcProblem* dev_group, int nprob,
                                  int64_t total_tiles, int num_sms, int* done,
-                                 cudaStream_t stream, int* err_flag);
+                                 cudaStream_t stream, int* err_flag, int* fix = nullptr);
 
 }  // namespace gb300
 }  // namespace t1m

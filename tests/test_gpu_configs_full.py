@@ -266,22 +266,26 @@ def _sweep_batch(torch, n_items, seed=2024):
 
 
 @pytest.mark.slow
-def test_config4_full_batch_grouped_graph(ctx, torch_cuda):
-    """All 1024 updates (2048 contractions) as one grouped launch under a CUDA
-    graph with the autotuner; every item's outputs checked against FP64 on
+@pytest.mark.parametrize("one_launch", [False, True], ids=["per-family", "one-launch"])
+def test_config4_full_batch_grouped_graph(ctx, torch_cuda, one_launch):
+    """All 1024 updates (2048 contractions) under a CUDA graph with the
+    autotuner, as family launches per level and as ONE persistent launch; every item's outputs checked against FP64 on
     sampled rows: R[x, s, :, :] (all y, b of one x, s) and O[x, :, :] for
     four x (all s, t; O rows hold only 2-4 entries, too few to normalise
     the error by on their own)."""
     import t1m_gb300 as t1m
     torch = torch_cuda
     items, keep = _sweep_batch(torch, 1024)
-    grp = t1m.Group(items, ctx=ctx, graph=True, autotune=True)
+    grp = t1m.Group(items, ctx=ctx, graph=True, autotune=True,
+                    options=t1m.GROUP_ONE_LAUNCH if one_launch else 0)
     try:
         grp.launch(timed=False)
-        grp.launch(timed=False)  # a graph replay over the same outputs
+        rep = grp.launch()  # a graph replay over the same outputs
         torch.cuda.synchronize()
     finally:
         grp.close()
+    # One persistent launch, or per level the family launches and reduction.
+    assert rep.kernels == 1 if one_launch else rep.kernels >= 2
     rng = np.random.default_rng(17)
     worst = (0.0, None)
     c128 = torch.complex128

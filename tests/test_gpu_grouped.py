@@ -134,11 +134,14 @@ def test_group_rejects_forward_dependency_and_host_data(ctx, torch_cuda):
         t1m.Group([(1.0, w(g[0]), "ab", w(g[1]), "bc", 0.0, w(g[2]), "ac", 1)], ctx=ctx)
 
 
-def test_group_split_k_long_contractions(ctx, torch_cuda):
+@pytest.mark.parametrize("one_launch", [False, True], ids=["per-family", "one-launch"])
+def test_group_split_k_long_contractions(ctx, torch_cuda, one_launch):
     """Items whose K exceeds the per-tile cap are split across CTAs (partials in
-    the group's workspace, one FP64 reduction per dependency level): a
-    tensor-core item, a skinny plain item, their dependents, complex alpha and
-    a nonzero beta applied by the reduction."""
+    the group's workspace): a wide item, a skinny item, their dependents,
+    complex alpha and a nonzero beta applied by the reduction.  As one
+    persistent launch the reduction runs in the kernel (the split that
+    finishes last sums the partials in FP64); per family, one FP64 reduction
+    launch per dependency level."""
     import t1m_gb300 as t1m
     torch = torch_cuda
     rng = np.random.default_rng(34)
@@ -161,10 +164,14 @@ def test_group_split_k_long_contractions(ctx, torch_cuda):
              (al, v(g["P"]), "xa", v(g["Q"]), "at", 0.5, v(r2), "xt", -1),
              (1.0, v(r1), "xy", v(g["Z"]), "yq", 0.0, v(o1), "xq", 0),
              (1.0, v(r2), "xt", v(g["W"]), "tz", 0.0, v(o2), "xz", 1)]
-    grp = t1m.Group(items, ctx=ctx, graph=True)
+    grp = t1m.Group(items, ctx=ctx, graph=True,
+                    options=t1m.GROUP_ONE_LAUNCH if one_launch else 0)
     rep = grp.launch()
-    # Two levels, each with main launches and one reduction.
-    assert rep.kernels >= 3
+    if not one_launch:
+        # Two levels, each with main launches and one reduction.
+        assert rep.kernels >= 3
+    else:
+        assert rep.kernels == 1
     d = lambda z: z.astype(np.complex128)  # noqa: E731
     R1 = d(X) @ d(Y)
     R2 = al * (d(P) @ d(Q)) + 0.5 * d(C0)
@@ -214,3 +221,108 @@ def test_group_skinny_outputs(ctx, torch_cuda, dt):
         mx, fro = no.rel_errors(gc.cpu().numpy().astype(np.complex128), ref)
         assert mx < tol and fro < tol, (mx, fro)
     grp.close()
+
+
+def _width_batch(torch, t1m, rng):
+    """complex64 items of every width class: N from 1 to 300 (ragged against
+    each tile width), TMA and gathered operands (row-major tensors, and a
+    permuted A), short and long K (split, reduced in the kernel), complex
+    alpha, nonzero beta, accumulation, conjugation, and items that read the
+    C of earlier items."""
+    d = lambda z: z.astype(np.complex128)  # noqa: E731
+    v = lambda z: t1m.tensor(list(z.shape), z, t1m.row_major)  # noqa: E731
+    items, checks, keep = [], [], []
+    specs = [  # (M, N, K, alpha, beta, flags)
+        (96, 1, 700, 1.0, 0.0, 0),
+        (200, 3, 5000, 0.5 - 0.25j, 0.5, 0),
+        (130, 13, 64, 1.0, 0.0, t1m.FLAG_CONJ_A),
+        (64, 16, 2100, 1.0, 0.25, t1m.FLAG_CONJ_B),
+        (77, 17, 48, 1j, 0.0, 0),
+        (150, 40, 3000, 1.0, 0.0, t1m.FLAG_ACCUMULATE),
+        (64, 64, 96, 1.0, 0.0, t1m.FLAG_CONJ_A | t1m.FLAG_CONJ_B),
+        (100, 100, 1030, 0.75, -0.5j, 0),
+        (257, 130, 80, 1.0, 0.0, 0),
+        (40, 300, 1500, 1.0, 0.0, 0),
+    ]
+    for (M, N, K, al, be, fl) in specs:
+        A = _rand(rng, (M, K), np.complex64, 0.2)
+        B = _rand(rng, (K, N), np.complex64, 0.2)
+        C0 = _rand(rng, (M, N), np.complex64, 1.0)
+        ga, gb, gc = (torch.from_numpy(x.copy()).cuda() for x in (A, B, C0))
+        a_ = d(A).conj() if fl & t1m.FLAG_CONJ_A else d(A)
+        b_ = d(B).conj() if fl & t1m.FLAG_CONJ_B else d(B)
+        prod = al * (a_ @ b_)
+        if fl & t1m.FLAG_ACCUMULATE:
+            ref = d(C0) + prod
+        else:
+            ref = prod + be * d(C0)
+        items.append((al, v(ga), "mk", v(gb), "kn", be, v(gc), "mn", -1, fl))
+        checks.append((gc, ref))
+        keep += [ga, gb]
+    # A permuted (gathered) A: labels "km" over a row-major (K, M) array.
+    M, N, K = 120, 24, 900
+    At = _rand(rng, (K, M), np.complex64, 0.2)
+    B = _rand(rng, (K, N), np.complex64, 0.2)
+    ga, gb = (torch.from_numpy(x.copy()).cuda() for x in (At, B))
+    gc = torch.zeros((M, N), dtype=torch.complex64, device="cuda")
+    items.append((1.0, v(ga), "km", v(gb), "kn", 0.0, v(gc), "mn", -1))
+    checks.append((gc, d(At).T @ d(B)))
+    keep += [ga, gb]
+    # Dependents: read the C of items 1 (N = 3, split) and 7 (N = 100).
+    for dep, (Md, Nd) in ((1, (200, 3)), (7, (100, 100))):
+        Q = _rand(rng, (Nd, 5), np.complex64, 0.2)
+        gq = torch.from_numpy(Q.copy()).cuda()
+        go = torch.zeros((Md, 5), dtype=torch.complex64, device="cuda")
+        items.append((1.0, items[dep][6], "mn", v(gq), "nq", 0.0, v(go), "mq", dep))
+        checks.append((go, checks[dep][1] @ d(Q)))
+        keep.append(gq)
+    return items, checks, keep
+
+
+@pytest.mark.parametrize("width", [0, 16, 32, 64, 128], ids=lambda w: f"w{w}" if w else "auto")
+def test_one_launch_tile_widths(ctx, torch_cuda, width):
+    """A complex64 batch under GROUP_ONE_LAUNCH is ONE persistent launch
+    (report: one kernel), each item with its own tile (chosen per item: SIMT
+    tiles for N <= 8, else a tensor-core width; or a width forced for all
+    items), long K split and reduced in the kernel, dependencies resolved in
+    the kernel; every output against FP64, on two launches in a row (the
+    in-kernel split counters reset themselves)."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    rng = np.random.default_rng(36)
+    items, checks, keep = _width_batch(torch, t1m, rng)
+    inits = [c.clone() for c, _ in checks]
+    grp = t1m.Group(items, ctx=ctx, graph=True, options=t1m.GROUP_ONE_LAUNCH | width)
+    for rnd in range(2):
+        for (c, _), c0 in zip(checks, inits):
+            c.copy_(c0)
+        torch.cuda.synchronize()
+        rep = grp.launch()
+        assert rep.kernels == 1
+        for i, (c, ref) in enumerate(checks):
+            mx, fro = no.rel_errors(c.cpu().numpy(), ref)
+            assert mx < 2e-6 and fro < 2e-6, (rnd, i, mx, fro)
+    grp.close()
+
+
+def test_one_launch_width_autotune(ctx, torch_cuda, tmp_path, monkeypatch):
+    """The autotuner picks a tile per shape class (a tensor-core width, or a
+    SIMT tile for outputs of at most 8 columns; cached in the tune file) and
+    the batch stays one launch with results within FP32 rounding of FP64."""
+    import t1m_gb300 as t1m
+    torch = torch_cuda
+    monkeypatch.setenv("T1M_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    rng = np.random.default_rng(37)
+    items, checks, keep = _width_batch(torch, t1m, rng)
+    grp = t1m.Group(items, ctx=ctx, graph=True, autotune=True, options=t1m.GROUP_ONE_LAUNCH)
+    rep = grp.launch()
+    assert rep.kernels == 1
+    for i, (c, ref) in enumerate(checks):
+        mx, fro = no.rel_errors(c.cpu().numpy(), ref)
+        assert mx < 2e-6 and fro < 2e-6, (i, mx, fro)
+    grp.close()
+    lines = (tmp_path / "tune.txt").read_text().splitlines()
+    # Tile choices: 1 = a SIMT tile (outputs of at most 8 columns), else the
+    # tensor-core tile width.
+    widths = [int(ln.split()[1]) for ln in lines[1:] if ln.startswith("w")]
+    assert widths and set(widths) <= {1, 16, 32, 64, 128}
