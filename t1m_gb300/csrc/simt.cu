@@ -90,6 +90,28 @@ __device__ __forceinline__ int64_t offs(const int64_t* v, int64_t u, int64_t i) 
 
 constexpr int kThreads = 256;
 
+// Global -> shared copy of one element (4, 8 or 16 bytes) that does not pass
+// through registers; src_bytes 0 writes zeros (operands past the tile edge).
+template <int kBytes>
+__device__ __forceinline__ void cp_async_elem(void* dst, const void* src, bool in) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  const uint32_t n = in ? kBytes : 0u;
+  if constexpr (kBytes == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n)
+                 : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src),
+                 "n"(kBytes), "r"(n)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit_group() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait_group() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 // 16 x 16 threads; thread (tx, ty) owns rows ty*TM .. ty*TM+TM-1 of the tile
 // and columns tx + 16*j (j < TN), so shared-memory reads of B are
 // consecutive across a half-warp and reads of A are broadcasts.
@@ -122,9 +144,17 @@ simt_contract(const GemmArgs args0, const SimtProblem* group, int nprob) {
 
   // Rows padded by 32 bytes: tile stores that walk k across threads (a
   // K-contiguous operand) then spread over the banks instead of hitting one.
+  // kStages tiles in flight: global -> shared copies by cp.async (no register
+  // staging, so the FMA loop never waits on a global load), zero-filled past
+  // the edges.
   constexpr int kPad = 32 / sizeof(T);
-  __shared__ __align__(16) T As[2][BK][BM + kPad];
-  __shared__ __align__(16) T Bs[2][BK][BN + kPad];
+  // Three stages where they fit the 48 KB of static shared memory and the
+  // registers (the grouped float instance spills with three), else two.
+  constexpr int kStageBytes = BK * (BM + BN + 2 * kPad) * static_cast<int>(sizeof(T));
+  constexpr int kStages =
+      (3 * kStageBytes <= 40 * 1024 && !(kGroup && sizeof(T) == 4)) ? 3 : 2;
+  __shared__ __align__(16) T As[kStages][BK][BM + kPad];
+  __shared__ __align__(16) T Bs[kStages][BK][BN + kPad];
   __shared__ int64_t rowA[BM];
   __shared__ int64_t colB[BN];
 
@@ -170,43 +200,41 @@ simt_contract(const GemmArgs args0, const SimtProblem* group, int nprob) {
   const bool a_kfast = (args.uA_k == 1);
   const bool b_kfast = (args.uB_k == 1) || (args.uB_n != 1);
 
-  T ra[A_PER], rb[B_PER];
-  auto load_tiles = [&](int64_t k0) {
+  auto issue_tiles = [&](int64_t k0, int buf) {
 #pragma unroll
     for (int p = 0; p < A_PER; ++p) {
       const int idx = tid + p * kThreads;
       const int m = a_kfast ? idx / BK : idx % BM;
       const int k = a_kfast ? idx % BK : idx / BM;
-      T v = zero<T>();
-      if (m0 + m < M && k0 + k < K)
-        v = conj_if(A[rowA[m] + offs(args.csA, args.uA_k, k0 + k)], conjA);
-      ra[p] = v;
+      const bool in = m0 + m < M && k0 + k < K;
+      const T* src = in ? A + rowA[m] + offs(args.csA, args.uA_k, k0 + k) : A;
+      cp_async_elem<sizeof(T)>(&As[buf][k][m], src, in);
     }
 #pragma unroll
     for (int p = 0; p < B_PER; ++p) {
       const int idx = tid + p * kThreads;
       const int n = b_kfast ? idx / BK : idx % BN;
       const int k = b_kfast ? idx % BK : idx / BN;
-      T v = zero<T>();
-      if (n0 + n < N && k0 + k < K)
-        v = conj_if(B[offs(args.rsB, args.uB_k, k0 + k) + colB[n]], conjB);
-      rb[p] = v;
+      const bool in = n0 + n < N && k0 + k < K;
+      const T* src = in ? B + offs(args.rsB, args.uB_k, k0 + k) + colB[n] : B;
+      cp_async_elem<sizeof(T)>(&Bs[buf][k][n], src, in);
     }
   };
-  auto store_tiles = [&](int buf) {
-#pragma unroll
-    for (int p = 0; p < A_PER; ++p) {
-      const int idx = tid + p * kThreads;
-      const int m = a_kfast ? idx / BK : idx % BM;
-      const int k = a_kfast ? idx % BK : idx / BM;
-      As[buf][k][m] = ra[p];
-    }
-#pragma unroll
-    for (int p = 0; p < B_PER; ++p) {
-      const int idx = tid + p * kThreads;
-      const int n = b_kfast ? idx / BK : idx % BN;
-      const int k = b_kfast ? idx % BK : idx / BN;
-      Bs[buf][k][n] = rb[p];
+  // Conjugation (complex types, rare: the adjoint) in shared memory, once
+  // per element of a landed stage, so the FMA loop stays free of it.
+  auto conj_stage = [&](int buf) {
+    if constexpr (Scalar<T>::cplx) {
+      if (conjA)
+        for (int e = tid; e < BK * BM; e += kThreads) {
+          T& v = As[buf][e / BM][e % BM];
+          v.y = -v.y;
+        }
+      if (conjB)
+        for (int e = tid; e < BK * BN; e += kThreads) {
+          T& v = Bs[buf][e / BN][e % BN];
+          v.y = -v.y;
+        }
+      if (conjA || conjB) __syncthreads();
     }
   };
 
@@ -217,14 +245,22 @@ simt_contract(const GemmArgs args0, const SimtProblem* group, int nprob) {
     for (int j = 0; j < TN; ++j) acc[i][j] = zero<T>();
 
   const int64_t ksteps = (K - kb + BK - 1) / BK;
-  if (ksteps > 0) {
-    load_tiles(kb);
-    store_tiles(0);
+  // Prologue: the first kStages - 1 stages in flight (one commit group each,
+  // empty groups past the end keep the group count aligned).
+#pragma unroll
+  for (int st = 0; st < kStages - 1; ++st) {
+    if (st < ksteps) issue_tiles(kb + st * BK, st);
+    cp_async_commit_group();
   }
-  __syncthreads();
   for (int64_t s = 0; s < ksteps; ++s) {
-    const int buf = static_cast<int>(s & 1);
-    if (s + 1 < ksteps) load_tiles(kb + (s + 1) * BK);
+    const int buf = static_cast<int>(s % kStages);
+    cp_async_wait_group<kStages - 2>();  // stage s has landed (this thread's copies)
+    __syncthreads();                     // ... and every thread's; stage s - 1 is consumed
+    conj_stage(buf);
+    // Refill the slot of stage s - 1 with stage s + kStages - 1.
+    const int64_t nxt = s + kStages - 1;
+    if (nxt < ksteps) issue_tiles(kb + nxt * BK, static_cast<int>(nxt % kStages));
+    cp_async_commit_group();
 #pragma unroll
     for (int k = 0; k < BK; ++k) {
       T a[TM], b[TN];
@@ -237,9 +273,8 @@ simt_contract(const GemmArgs args0, const SimtProblem* group, int nprob) {
 #pragma unroll
         for (int j = 0; j < TN; ++j) mac(acc[i][j], a[i], b[j]);
     }
-    if (s + 1 < ksteps) store_tiles(buf ^ 1);
-    __syncthreads();
   }
+  cp_async_wait_group<0>();
 
   // Epilogue: scatter-write C with alpha/beta.
   const T alpha = scal<T>(args.alpha);
