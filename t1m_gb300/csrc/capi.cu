@@ -672,7 +672,20 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
   cudaEventRecord(ctx->pev[kEvRes], ctx->copy_in);
   if (res_pieces && (e = split_resident(0)) != cudaSuccess)
     return cuda_fail(ctx, e, "split resident operand");
-  const int early = split ? std::min(2, sl.count) : 0;  // slabs before the second half
+  // Slabs before the second half: blocks of the first half keep the GPU busy
+  // while the second half of the resident operand is copied.  When the
+  // product's compute (estimated at 200 TFLOP/s on the tensor cores, 40 on
+  // the plain kernel) outlasts the copies of all its operands, every slab's
+  // first-half block goes first (the second half then arrives long before
+  // the first-half blocks end); otherwise two, so that C slabs start going
+  // back early.  Complex64 4096^3 (2.0 ms of compute, 1.3 ms of copies in):
+  // two slabs left the GPU idle for about 0.2 ms while the second half of A
+  // was in flight.
+  const bool cplx = dtype == T1M_COMPLEX64 || dtype == T1M_COMPLEX128;
+  const double est_flops = (cplx ? 8.0 : 2.0) * double(hp.M) * double(hp.N) * double(hp.K);
+  const double est_compute_s = est_flops / (method == T1M_METHOD_PLAIN ? 40e12 : 200e12);
+  const double est_copy_s = double(bytesA + bytesB + (readC ? bytesC : 0)) / 200e9;
+  const int early = !split ? 0 : est_compute_s > est_copy_s ? sl.count : std::min(2, sl.count);
   for (int i = 0; i < early; ++i) {
     if ((e = copy_slab(i)) != cudaSuccess) return cuda_fail(ctx, e, "copy slab to device");
     if (int st = launch_block(i, 0)) return st;
