@@ -606,6 +606,37 @@ def workload_c128(args):
                       "cases": out}), flush=True)
 
 
+def workload_plain(args):
+    """The plain FP32 form alone on the headline workload (complex64
+    ijkl,klmn->ijmn, extents --extent, col-major): TFLOP/s and its fraction
+    of the nominal FP32 SIMT peak (the command the plain kernel's profile is
+    taken with)."""
+    import torch
+    import t1m_gb300 as t1m
+    E = args.extent
+    ctx = t1m.Context()
+    ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(3)
+    n = E ** 4
+    mk = lambda: torch.complex(torch.rand(n, device="cuda", generator=g) * 2 - 1,  # noqa: E731
+                               torch.rand(n, device="cuda", generator=g) * 2 - 1)
+    ga, gb = mk(), mk()
+    gc = torch.zeros(n, dtype=torch.complex64, device="cuda")
+    ta, tb, tc = (t1m.tensor([E] * 4, x) for x in (ga, gb, gc))
+    ctx.set_method("plain")
+    ms = _events_ms(torch, lambda: t1m.contract_raw(1.0, ta, LA, tb, LB, 0.0, tc, LC,
+                                                   t1m.FLAG_NO_TIMING, ctx),
+                    args.steps, args.warmup)
+    flops = 8.0 * float(E ** 2) ** 3
+    nominal = 152 * 128 * 2 * 2.07e9 / 1e12
+    ctx.close()
+    print(json.dumps({"workload": f"plain FP32 form, complex64 ijkl,klmn->ijmn extents {E}, col-major",
+                      "ms": ms, "tflops": flops / ms / 1e9,
+                      "frac_of_fp32_simt_nominal": flops / ms / 1e9 / nominal,
+                      "fp32_simt_nominal_tflops": nominal}), flush=True)
+
+
 def workload_batch(args):
     """Batching form: 1024 updates xay,asb->xsyb then xsyb,ytb->xst with
     x, y, a, b ~ U{16..256 step 16}, s, t ~ U{2, 4}, components N(0, 1/sqrt(bond));
@@ -744,8 +775,10 @@ def main() -> None:
                     help="tune tile form and split count per shape class (first call)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="headline",
-                    choices=["headline", "config2", "logmag", "c128", "batch", "vjp"])
+                    choices=["headline", "config2", "logmag", "c128", "batch", "vjp", "plain"])
     ap.add_argument("--items", type=int, default=1024)
+    ap.add_argument("--extent", type=int, default=64,
+                    help="plain workload: every extent of ijkl,klmn->ijmn")
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch workload: heuristic kernel families instead of the autotuner")
     args = ap.parse_args()
@@ -759,7 +792,7 @@ def main() -> None:
         # t1m_set_stream reads as "the context's own") keeps both on one.
         import torch
         fn = {"config2": workload_config2, "logmag": workload_logmag, "c128": workload_c128,
-              "batch": workload_batch, "vjp": workload_vjp}[args.workload]
+              "batch": workload_batch, "vjp": workload_vjp, "plain": workload_plain}[args.workload]
         with torch.cuda.stream(torch.cuda.Stream()):
             fn(args)
     else:

@@ -72,6 +72,12 @@ struct t1m_context {
   void* res_pieces = nullptr;
   size_t res_pieces_bytes = 0;
   int split_k = 0;
+  // Arrival counters of the persistent kernel's in-kernel split-K reduction
+  // (zeroed when allocated; the kernel leaves them at zero; zeroed again
+  // after a kernel reported an error).
+  int* fix_ctr = nullptr;
+  int64_t fix_cap = 0;
+  bool fix_dirty = false;
   // Cap on each optional workspace (panels, packs); -1 = none.
   int64_t opt_work_limit = -1;
   // T1M_TILE_* form of tensor-core products.
@@ -235,6 +241,7 @@ int check_device_error(t1m_context* ctx) {
   if (e != cudaSuccess) return cuda_fail(ctx, e, "read kernel status");
   if (code == 0) return T1M_OK;
   cudaMemset(ctx->d_err, 0, sizeof(int));
+  ctx->fix_dirty = true;  // a kernel cut short may leave arrival counters set
   return fail(ctx, T1M_ERR_KERNEL_TIMEOUT,
               "a bounded device-side wait timed out (kernel code " + std::to_string(code) + ")");
 }
@@ -335,6 +342,7 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
                    const PiecesReady* ready = nullptr) {
   int nk = 0;
   int splits = 1;
+  bool reduced = false;  // the split product was reduced inside its kernel
   cudaError_t e = cudaSuccess;
   if (g.K == 0) {
     // C <- beta*C (or unchanged): nothing to multiply; handled by the plain
@@ -405,15 +413,34 @@ int launch_product(t1m_context* ctx, int method, int dtype, size_t es, const Hos
       const size_t kb = tc_pack_bytes(dtype, hp);
       const bool pk = kb > 0 && within(kb) &&
                       ensure_opt_work(s, &ctx->pack[slot], &ctx->pack_bytes[slot], kb);
+      // Arrival counters for the persistent kernel's in-kernel reduction of
+      // a split product (the one-tile forms use the reduction kernel).
+      constexpr int64_t kFixCap = int64_t(1) << 16;
+      if (splits > 1 && !ctx->fix_ctr) {
+        if (cudaMalloc(&ctx->fix_ctr, sizeof(int) * kFixCap) == cudaSuccess &&
+            cudaMemset(ctx->fix_ctr, 0, sizeof(int) * kFixCap) == cudaSuccess) {
+          ctx->fix_cap = kFixCap;
+        } else {
+          cudaGetLastError();
+          if (ctx->fix_ctr) cudaFree(ctx->fix_ctr);
+          ctx->fix_ctr = nullptr;
+        }
+      }
+      if (ctx->fix_dirty && ctx->fix_ctr) {
+        cudaMemsetAsync(ctx->fix_ctr, 0, sizeof(int) * size_t(ctx->fix_cap), s);
+        ctx->fix_dirty = false;
+      }
+      TcFix fix{splits > 1 ? ctx->fix_ctr : nullptr, ctx->fix_cap, &g, false};
       e = launch_tc(method, dtype, gm, hp, splits, s, ctx->d_err, &nk, &err, &ran,
                     pan ? ctx->panel[slot] : nullptr, pan ? ctx->panel_bytes[slot] : 0,
                     pk ? ctx->pack[slot] : nullptr, pk ? ctx->pack_bytes[slot] : 0,
-                    &ctx->last_path, form, ready, ctx->mev_armed ? ctx->mev : nullptr);
+                    &ctx->last_path, form, ready, ctx->mev_armed ? ctx->mev : nullptr, &fix);
+      reduced = fix.reduced;
       if (e == cudaSuccess && ctx->mev_armed) ctx->mev_recorded = true;
       *used_method = ran;
       if (e != cudaSuccess && !err.empty()) return fail(ctx, T1M_ERR_CUDA, err);
     }
-    if (e == cudaSuccess && splits > 1) {
+    if (e == cudaSuccess && splits > 1 && !reduced) {
       e = launch_splitk_reduce(dtype, ctx->work, splits, g, s);
       ++nk;
     }
@@ -847,6 +874,7 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->mev[i]) cudaEventDestroy(ctx->mev[i]);
   if (ctx->d_err) cudaFree(ctx->d_err);
   if (ctx->work) cudaFree(ctx->work);
+  if (ctx->fix_ctr) cudaFree(ctx->fix_ctr);
   for (int i = 0; i < 2; ++i) {
     if (ctx->panel[i]) cudaFree(ctx->panel[i]);
     if (ctx->pack[i]) cudaFree(ctx->pack[i]);

@@ -218,12 +218,23 @@ struct PiecesReady {
 // `main_ev` (may be null): two events recorded on `stream` right before and
 // after the launch of the product's main kernel (after its split, pack and
 // panel passes).
+// In-kernel split-K reduction of a split product on the persistent kernel:
+// `ctr` (cap zeroed ints) for the arrival counters, `out` the product's own
+// arguments (C, alpha, beta, flags); launch_tc sets `reduced` when the kernel
+// applied the epilogue itself (no reduction kernel needed).
+struct TcFix {
+  int* ctr;
+  int64_t cap;
+  const GemmArgs* out;
+  bool reduced;
+};
 cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPlan& plan,
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel = nullptr,
                       size_t panel_bytes = 0, void* pack = nullptr, size_t pack_bytes = 0,
                       int* path = nullptr, int form = 0 /* T1M_TILE_* */,
-                      const PiecesReady* ready = nullptr, cudaEvent_t* main_ev = nullptr);
+                      const PiecesReady* ready = nullptr, cudaEvent_t* main_ev = nullptr,
+                      TcFix* fix = nullptr);
 // Panel workspace a product would use (0: panels not used at this size).
 size_t tc_panel_bytes(int dtype, int64_t M, int64_t N, int64_t K);
 // Bytes of the operand pieces of the T1M_TILE_PIECES form (held in the panel

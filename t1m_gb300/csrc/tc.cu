@@ -80,6 +80,9 @@ constexpr int kRaw = 4;         // raw tile stages
 constexpr int kStages = 2;      // converted operand stages
 constexpr int kFold = 4;        // stages per chunk accumulator (128 real K)
 constexpr int kSkinnyTcN = 8;   // columns of a SIMT tile of the persistent kernel
+// Longest in-kernel split-K reduction a single product takes (partials read
+// per thread of the last split's CTA); longer ones use the reduction kernel.
+constexpr int64_t kFixMaxLoads = 64;
 static_assert(kSkinnyTcN == kTcSkinnyMaxN, "SIMT tile width");
 constexpr int kThreads = 384;   // warp 0: MMA; warps 1-3: loaders; 4-11: converters
 constexpr int kLoaderBase = 32;
@@ -563,12 +566,17 @@ __device__ __forceinline__ TileRef locate(const TcProblem* single, const TcProbl
 
 // In-kernel split-K reduction of one output tile (the converter warps of the
 // split that arrived last, pt = 0..255): C(m, n) <- alpha * sum_s W_s(m, n)
-// + beta * C(m, n) (or C + alpha * sum), the sum over the splits in order
-// and the epilogue in FP64, as the separate reduction kernel does.  The
-// partials are the raw products written through p.g (dense, uniform
-// strides, c_split_stride apart); other CTAs wrote them, so they are read
-// from L2 (ld.global.cg).  Thread pt takes row m0 + pt % 64 and columns
-// n0 + pt / 64, + 4, ... of the tile.
+// + beta * C(m, n) (or C + alpha * sum), the sum and the epilogue in FP64.
+// The summation order is the reduction kernel's (splitk.cu): G = 2, 4 or 8
+// groups, group g summing the slices g, g + G, ... in ascending order, then
+// the G group sums in group order; and its epilogue expressions, so both
+// paths give the same result.  The partials are the raw products written
+// through p.g (dense, uniform strides, c_split_stride apart); other CTAs
+// wrote them, so they are read from L2 (ld.global.cg).  Thread pt takes row
+// m0 + pt % 64 and columns n0 + pt / 64, + 4, ... of the tile.
+__device__ __forceinline__ double2 fix_cmul(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
 __device__ __noinline__ void fix_reduce_tile(const TcProblem& p, const TileRef& tr, int pt) {
   const GemmArgs& w = p.g;
   const GemmArgs& o = p.out;
@@ -579,28 +587,40 @@ __device__ __noinline__ void fix_reduce_tile(const TcProblem& p, const TileRef& 
   const int64_t wm = m * w.uC_m;
   const int64_t om = offs(o.rsC, o.uC_m, m);
   const int splits = p.splits;
-  const double ar = o.alpha[0], ai = o.alpha[1], br = o.beta[0], bi = o.beta[1];
+  const int G = splits <= 2 ? 2 : splits <= 4 ? 4 : 8;
+  const double2 alpha = make_double2(o.alpha[0], o.alpha[1]);
+  const double2 beta = make_double2(o.beta[0], o.beta[1]);
   for (int64_t n = tr.n0 + (pt >> 6); n < n_end; n += 4) {
     const float2* src = W + wm + n * w.uC_n;
-    double sr = 0.0, si = 0.0;
+    double2 tot = make_double2(0.0, 0.0);
+    for (int gi = 0; gi < G; ++gi) {
+      double2 acc = make_double2(0.0, 0.0);
 #pragma unroll 4
-    for (int sp = 0; sp < splits; ++sp) {
-      const float2 v = __ldcg(src + static_cast<int64_t>(sp) * w.c_split_stride);
-      sr += static_cast<double>(v.x);
-      si += static_cast<double>(v.y);
+      for (int sp = gi; sp < splits; sp += G) {
+        const float2 v = __ldcg(src + static_cast<int64_t>(sp) * w.c_split_stride);
+        acc.x += static_cast<double>(v.x);
+        acc.y += static_cast<double>(v.y);
+      }
+      if (gi == 0) {
+        tot = acc;
+      } else {
+        tot.x += acc.x;
+        tot.y += acc.y;
+      }
     }
     float2* dst = static_cast<float2*>(o.C) + om + offs(o.csC, o.uC_n, n);
-    double rr = ar * sr - ai * si, ri = ar * si + ai * sr;
+    double2 r = fix_cmul(alpha, tot);
     if (o.flags & kFlagAccumulate) {
       const float2 c = *dst;
-      rr += c.x;
-      ri += c.y;
+      r.x += static_cast<double>(c.x);
+      r.y += static_cast<double>(c.y);
     } else if (!(o.flags & kFlagBetaZero)) {
       const float2 c = *dst;
-      rr += br * c.x - bi * c.y;
-      ri += br * c.y + bi * c.x;
+      const double2 bc = fix_cmul(beta, make_double2(c.x, c.y));
+      r.x += bc.x;
+      r.y += bc.y;
     }
-    *dst = make_float2(static_cast<float>(rr), static_cast<float>(ri));
+    *dst = make_float2(static_cast<float>(r.x), static_cast<float>(r.y));
   }
 }
 
@@ -3142,7 +3162,7 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
                       int splits, cudaStream_t stream, int* err_flag, int* kernels,
                       std::string* err, int* used_method, void* panel, size_t panel_bytes,
                       void* pack, size_t pack_bytes, int* path, int form,
-                      const PiecesReady* ready, cudaEvent_t* main_ev) {
+                      const PiecesReady* ready, cudaEvent_t* main_ev, TcFix* fix) {
   *kernels = 0;
   auto mark = [&](int i) {
     if (main_ev) cudaEventRecord(main_ev[i], stream);
@@ -3401,8 +3421,26 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     }
     p.tile_begin = 0;
     p.dep = -1;
+    // A split product is reduced in the kernel (the last split of each
+    // output tile sums all partials in FP64 and applies the epilogue)
+    // instead of by a reduction launch.
+    // Only where that reduction is short: the last split's 256 threads read
+    // ceil(width / 4) x splits partials each, dependent on one CTA per output
+    // tile; abcd,dbea->ec (2 output tiles of 64 columns, 75 splits: 1200
+    // partials per thread) took 464 us that way against 70 us with the
+    // reduction kernel spread over the GPU.
+    const int64_t fix_loads = (std::min<int64_t>(p.tile_n, p.g.N) + 3) / 4 * splits;
+    int* fix_ctr = nullptr;
+    if (fix && fix->ctr && fix->out && splits > 1 && fix_loads <= kFixMaxLoads &&
+        int64_t(p.tiles_m) * p.tiles_n <= fix->cap) {
+      p.fix_begin = 0;
+      p.out = *fix->out;
+      fix_ctr = fix->ctr;
+      fix->reduced = true;
+    }
     mark(0);
-    e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag);
+    e = tc_launch_persistent(&p, nullptr, 1, tc_problem_tiles(p), sms, nullptr, stream, err_flag,
+                             fix_ctr);
     mark(1);
     set_path(p.amode, p.bmode, true, packed_args.A != args.A, packed_args.B != args.B);
   }
