@@ -1230,57 +1230,57 @@ tc3xtf32_persistent(const __grid_constant__ TcProblem single, const TcProblem* g
         ok = run_skinny(tr, alay, blay, conjA, conjB, Cp);
         if (!ok) break;
       } else {
-      cur_tn = tr.tn;
+        cur_tn = tr.tn;
 #pragma unroll
-      for (int j = 0; j < 64; ++j) master[j] = 0.f;
-      const int64_t chunk_base = chunk_cnt;
-      using I0 = std::integral_constant<int, 0>;
-      using I1 = std::integral_constant<int, 1>;
-      using I2 = std::integral_constant<int, 2>;
-      using I3 = std::integral_constant<int, 3>;
-      switch (alay * 4 + blay) {
-        case 0: ok = run_stages(I0{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 1: ok = run_stages(I0{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 3: ok = run_stages(I0{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 4: ok = run_stages(I1{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 5: ok = run_stages(I1{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 7: ok = run_stages(I1{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 8: ok = run_stages(I2{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        case 9: ok = run_stages(I2{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
-        default: ok = run_stages(I2{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
-      }
-      if (!ok) break;
+        for (int j = 0; j < 64; ++j) master[j] = 0.f;
+        const int64_t chunk_base = chunk_cnt;
+        using I0 = std::integral_constant<int, 0>;
+        using I1 = std::integral_constant<int, 1>;
+        using I2 = std::integral_constant<int, 2>;
+        using I3 = std::integral_constant<int, 3>;
+        switch (alay * 4 + blay) {
+          case 0: ok = run_stages(I0{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          case 1: ok = run_stages(I0{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          case 3: ok = run_stages(I0{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          case 4: ok = run_stages(I1{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          case 5: ok = run_stages(I1{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          case 7: ok = run_stages(I1{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          case 8: ok = run_stages(I2{}, I0{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          case 9: ok = run_stages(I2{}, I1{}, tr, conjA, conjB, row_ok, chunk_base); break;
+          default: ok = run_stages(I2{}, I3{}, tr, conjA, conjB, row_ok, chunk_base); break;
+        }
+        if (!ok) break;
 
-      // -------------------------------------------------------- epilogue ---
-      if (!ptx::mbar_wait(acc_full, static_cast<uint32_t>(tile_cnt & 1))) {
-        record_error(err_flag, kErrAccWait);
-        ok = false;
-        break;
-      }
-      ptx::tc_fence_after();
-      // The last chunk of the tile was not folded in the loop; then the
-      // corrections.  After these reads the accumulators are free again.
-      const int64_t c_last = chunk_base + (tr.ksteps > 0 ? (tr.ksteps - 1) >> tr.fsh : 0);
-      const int buf_last = static_cast<int>(c_last & 1);
-      // An empty K range (K = 0) leaves the accumulators unwritten: nothing
-      // is folded (C = beta C), but the arrivals below keep the barrier
-      // phases of both sides in step (the MMA thread counts a chunk too).
-      if (tr.ksteps > 0) {
-        fold_from(buf_last ? kChunkCol1 : kChunkCol0);
-        fold_from(kCorrCol);
-      }
-      ptx::tc_fence_before();
-      __syncwarp();
-      if (lane == 0) {
-        ptx::mbar_arrive(chunk_empty(buf_last));
-        ptx::mbar_arrive(acc_empty);
-      }
-      chunk_cnt = c_last + 1;
-      ++tile_cnt;
+        // -------------------------------------------------------- epilogue ---
+        if (!ptx::mbar_wait(acc_full, static_cast<uint32_t>(tile_cnt & 1))) {
+          record_error(err_flag, kErrAccWait);
+          ok = false;
+          break;
+        }
+        ptx::tc_fence_after();
+        // The last chunk of the tile was not folded in the loop; then the
+        // corrections.  After these reads the accumulators are free again.
+        const int64_t c_last = chunk_base + (tr.ksteps > 0 ? (tr.ksteps - 1) >> tr.fsh : 0);
+        const int buf_last = static_cast<int>(c_last & 1);
+        // An empty K range (K = 0) leaves the accumulators unwritten: nothing
+        // is folded (C = beta C), but the arrivals below keep the barrier
+        // phases of both sides in step (the MMA thread counts a chunk too).
+        if (tr.ksteps > 0) {
+          fold_from(buf_last ? kChunkCol1 : kChunkCol0);
+          fold_from(kCorrCol);
+        }
+        ptx::tc_fence_before();
+        __syncwarp();
+        if (lane == 0) {
+          ptx::mbar_arrive(chunk_empty(buf_last));
+          ptx::mbar_arrive(acc_empty);
+        }
+        chunk_cnt = c_last + 1;
+        ++tile_cnt;
 
-      if (64 * wg < tr.tn)
-        store_tile<64>(g, Cp, tr.m0 + ci, row_ok, tr.n0, wg * 64, part, master,
-                       tr.n0 + tr.tn);
+        if (64 * wg < tr.tn)
+          store_tile<64>(g, Cp, tr.m0 + ci, row_ok, tr.n0, wg * 64, part, master,
+                         tr.n0 + tr.tn);
       }
       bool final_tile = true;
       if (fix && p->fix_begin >= 0) {
