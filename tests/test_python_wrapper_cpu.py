@@ -63,3 +63,25 @@ def test_scalar_encoding():
     assert list(t1m._scalar_bytes(t1m.COMPLEX64, 1 - 2j)) == [1.0, -2.0]
     assert list(t1m._scalar_bytes(t1m.FLOAT64, 3.5)) == [3.5]
     assert C.sizeof(t1m._scalar_bytes(t1m.COMPLEX128, 1j)) == 16
+
+
+def test_constants_mirror_the_c_header():
+    """Every T1M_FLAG_*, T1M_GROUP_* and T1M_PATH_* flag of include/t1m_capi.h
+    has the same value in the Python mirror (GROUP_*, FLAG_*, PATH_*), and the
+    tile forms match T1M_TILE_*."""
+    import re
+    from pathlib import Path
+
+    import t1m_gb300 as t1m
+    hdr = (Path(__file__).resolve().parents[1] / "include" / "t1m_capi.h").read_text()
+    defs = {m.group(1): int(m.group(2), 0)
+            for m in re.finditer(r"^#define T1M_(\w+) (0x[0-9A-Fa-f]+|\d+)u?\b", hdr, re.M)}
+    checked = 0
+    for name, value in defs.items():
+        if name.startswith(("FLAG_", "GROUP_", "PATH_")) and name != "PATH_B_PANELS":
+            assert getattr(t1m, name) == value, name
+            checked += 1
+        elif name.startswith("TILE_"):
+            assert t1m.TILE_FORMS[name[5:].lower()] == value, name
+            checked += 1
+    assert checked >= 20, checked
