@@ -71,6 +71,9 @@ struct t1m_context {
   // every slab (grow only; an optional workspace like the panels).
   void* res_pieces = nullptr;
   size_t res_pieces_bytes = 0;
+  // ... and of its streamed operand, each slab split once for both halves.
+  void* slab_pieces = nullptr;
+  size_t slab_pieces_bytes = 0;
   int split_k = 0;
   // Arrival counters of the persistent kernel's in-kernel split-K reduction
   // (zeroed when allocated; the kernel leaves them at zero; zeroed again
@@ -99,7 +102,7 @@ struct t1m_context {
   // between the context stream and this one, so the last wave of one slab's
   // kernel shares the SMs with the first of the next.
   cudaStream_t compute2 = nullptr;
-  static constexpr int kPipeEvents = 3 + 8 + 2 * 8 + 2 + 2;
+  static constexpr int kPipeEvents = 3 + 8 + 2 * 8 + 2 + 2 + 8;
   cudaEvent_t pev[kPipeEvents] = {};
 };
 
@@ -528,7 +531,8 @@ enum : int {
   kEvOut = kEvDone + 2 * kMaxSlabs,  // copy_out finished
   kEvC2 = kEvOut + 1,                // compute2 finished
   kEvResPieces = kEvC2 + 1,          // + h: pieces of resident half h split
-  kEvCount = kEvResPieces + 2
+  kEvSlabPieces = kEvResPieces + 2,  // + i: pieces of streamed slab i split
+  kEvCount = kEvSlabPieces + kMaxSlabs
 };
 static_assert(kEvCount <= t1m_context::kPipeEvents, "pipeline events");
 
@@ -660,6 +664,21 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
     cudaEventRecord(ctx->pev[kEvResPieces + h], s);
     return r;
   };
+  // The streamed operand's pieces: with the resident operand in halves, a
+  // slab is used by two blocks; its first block splits it once into its own
+  // rows of this workspace and the other block reuses them (the per-block
+  // split did it twice: 16 splits of 42 MB moved at 4096^3 instead of 8).
+  const int64_t srows = sl.along_n ? hp.N : 2 * hp.M;  // rows of the streamed pieces
+  const size_t sbytes = size_t(npieces) * size_t(srows) * size_t(ppitch) * 2u;
+  const bool slab_pieces =
+      res_pieces && split &&
+      (ctx->opt_work_limit < 0 || pbytes + sbytes <= size_t(ctx->opt_work_limit)) &&
+      ensure_opt_work(s, &ctx->slab_pieces, &ctx->slab_pieces_bytes, sbytes);
+  auto slab_row0 = [&](int i) -> int64_t {
+    const int64_t lo = i * sl.width;
+    return (sl.along_n ? lo : 2 * lo) * ppitch;
+  };
+  std::vector<char> slab_split(sl.count, 0);
   auto launch_block = [&](int i, int h) -> int {
     const int slot = nblock++ & 1;
     cudaStream_t cs = slot ? ctx->compute2 : s;
@@ -675,6 +694,25 @@ int run_pipelined(t1m_context* ctx, int method, int dtype, size_t es, const Host
       } else {
         ready.b = p;
         ready.b_plane = prows * ppitch;
+      }
+    }
+    if (slab_pieces) {
+      void* sp = static_cast<uint16_t*>(ctx->slab_pieces) + slab_row0(i);
+      if (!slab_split[i]) {
+        const cudaError_t r = tc_split_operand(npieces, !sl.along_n, gs, sp, srows * ppitch, cs);
+        if (r != cudaSuccess) return cuda_fail(ctx, r, "split streamed slab");
+        ++kernels;
+        cudaEventRecord(ctx->pev[kEvSlabPieces + i], cs);
+        slab_split[i] = 1;
+      } else {
+        cudaStreamWaitEvent(cs, ctx->pev[kEvSlabPieces + i], 0);
+      }
+      if (sl.along_n) {
+        ready.b = sp;
+        ready.b_plane = srows * ppitch;
+      } else {
+        ready.a = sp;
+        ready.a_plane = srows * ppitch;
       }
     }
     if (int st = launch_product(ctx, method, dtype, es, hp, gs, cs, &kernels, &used_method,
@@ -880,6 +918,7 @@ int t1m_destroy(t1m_context* ctx) {
     if (ctx->pack[i]) cudaFree(ctx->pack[i]);
   }
   if (ctx->res_pieces) cudaFree(ctx->res_pieces);
+  if (ctx->slab_pieces) cudaFree(ctx->slab_pieces);
   if (ctx->compute2) {
     cudaStreamSynchronize(ctx->compute2);
     cudaStreamDestroy(ctx->compute2);
