@@ -270,9 +270,9 @@ typedef struct t1m_group t1m_group;
 #define T1M_GROUP_INJECT_UNMET_DEPENDENCY 4u
 /* complex64 batches as one persistent launch (see above). */
 #define T1M_GROUP_ONE_LAUNCH 8u
-/* One-launch batches: every item's tile forced to 16, 32, 64 or 128 output
- * columns on the tensor cores (exactly one of these bits; tests and
- * measurements). */
+/* One-launch batches: the tile of every item with more than 8 output columns
+ * forced to 16, 32, 64 or 128 columns on the tensor cores (exactly one of
+ * these bits; tests and measurements); narrower outputs stay SIMT tiles. */
 #define T1M_GROUP_TILE_16 16u
 #define T1M_GROUP_TILE_32 32u
 #define T1M_GROUP_TILE_64 64u

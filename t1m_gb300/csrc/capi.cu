@@ -1764,9 +1764,12 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
       const GemmArgs probe = split_args(args[i], scratch, kps);
       float best = 1e30f;
       int best_w = width[i];
+      // Outputs of at most kTcSkinnyMaxN columns are SIMT tiles (see the
+      // forced widths below); wider ones try every width they can use.
       std::vector<int> cands;
       if (hp.N <= kTcSkinnyMaxN) cands.push_back(kWidthSimt);
       for (int w : kTcTileWidths) {
+        if (hp.N <= kTcSkinnyMaxN) break;
         if (w > 16 && w / 2 >= hp.N) break;  // wider than the output needs
         cands.push_back(w);
       }
@@ -1811,7 +1814,13 @@ extern "C" int t1m_group_create(t1m_context* ctx, int dtype, int n, const t1m_gr
     if (fw != T1M_GROUP_TILE_16 && fw != T1M_GROUP_TILE_32 && fw != T1M_GROUP_TILE_64 &&
         fw != T1M_GROUP_TILE_128)
       return fail(ctx, T1M_ERR_INVALID_ARGUMENT, "more than one tile width option");
-    std::fill(width.begin(), width.end(), static_cast<int>(fw));
+    // Outputs of at most kTcSkinnyMaxN columns stay SIMT tiles: a batch with
+    // N = 2, 5 and 8 items on forced 16-column tensor-core tiles raised an
+    // unspecified launch failure whose cause reading the code did not show
+    // (N = 1 and 3 items on the same tiles, and all of them as SIMT tiles,
+    // ran correctly), so narrow outputs do not take that form.
+    for (int i = 0; i < n; ++i)
+      if (width[i] != kWidthSimt) width[i] = static_cast<int>(fw);
   }
 
   // Autotuning of family launches: per shape class, time the candidate

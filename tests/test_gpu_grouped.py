@@ -283,8 +283,8 @@ def _width_batch(torch, t1m, rng):
 def test_one_launch_tile_widths(ctx, torch_cuda, width):
     """A complex64 batch under GROUP_ONE_LAUNCH is ONE persistent launch
     (report: one kernel), each item with its own tile (chosen per item: SIMT
-    tiles for N <= 8, else a tensor-core width; or a width forced for all
-    items), long K split and reduced in the kernel, dependencies resolved in
+    tiles for N <= 8, else a tensor-core width; or a width forced for every
+    item wider than 8 columns), long K split and reduced in the kernel, dependencies resolved in
     the kernel; every output against FP64, on two launches in a row (the
     in-kernel split counters reset themselves)."""
     import t1m_gb300 as t1m
