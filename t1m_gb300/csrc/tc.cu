@@ -3415,7 +3415,11 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     // The persistent kernel takes narrower output tiles where the output
     // has few columns (abcd,dbea->ec: N = 64 in one 64-column tile instead
     // of half a 128-column tile).
-    if (const int w = tc_default_tile_n(p.g.N); w != p.tile_n) {
+    // (Outputs of at most kTcSkinnyMaxN columns keep the 128-column tile:
+    // narrow tensor-core tiles for them are not run, see tc_prepare's tile
+    // width in grouped launches.)
+    if (const int w = p.g.N > kTcSkinnyMaxN ? tc_default_tile_n(p.g.N) : p.tile_n;
+        w != p.tile_n) {
       TcProblem q;
       if (tc_prepare(packed_args, *packed_plan, splits, &q, w)) p = q;
     }
