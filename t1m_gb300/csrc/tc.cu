@@ -3415,9 +3415,10 @@ cudaError_t launch_tc(int method, int dtype, const GemmArgs& args, const HostPla
     // The persistent kernel takes narrower output tiles where the output
     // has few columns (abcd,dbea->ec: N = 64 in one 64-column tile instead
     // of half a 128-column tile).
-    // (Outputs of at most kTcSkinnyMaxN columns keep the 128-column tile:
-    // narrow tensor-core tiles for them are not run, see tc_prepare's tile
-    // width in grouped launches.)
+    // Outputs of at most kTcSkinnyMaxN columns keep the 128-column tile:
+    // 16-column tensor-core tiles for such outputs (N = 2, 5, 8) raised an
+    // unspecified launch failure in a grouped launch, cause not found, so
+    // they are not run.
     if (const int w = p.g.N > kTcSkinnyMaxN ? tc_default_tile_n(p.g.N) : p.tile_n;
         w != p.tile_n) {
       TcProblem q;
